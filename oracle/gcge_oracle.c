@@ -1,0 +1,855 @@
+/*
+ * gcge_oracle.c -- CPU restatement of GCGE-1.0's CSR eigensolver path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle): loaded by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg, never by the
+ * product library.
+ *
+ * The reference keeps multivectors as arrays of independent column pointers
+ * and exchanges columns by swapping pointers; this restatement does the same
+ * (mv_t below) so that every phase of GCGE_Solve can be followed one to one.
+ * Dense small-matrix work goes to LAPACK/BLAS exactly where the reference
+ * calls it (dsyevx, dgemm, dsymm, ddot, dnrm2, dscal); they are taken from
+ * SciPy's bundled OpenBLAS (symbols with the scipy_ prefix), the same library
+ * the reference build in oracle/_ref links.
+ */
+#define _POSIX_C_SOURCE 199309L
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "gcge_oracle.h"
+
+/* ------------------------------------------------------------------ LAPACK */
+extern void scipy_dsyevx_(char *jobz, char *range, char *uplo, int *n, double *a, int *lda,
+                          double *vl, double *vu, int *il, int *iu, double *abstol, int *m,
+                          double *w, double *z, int *ldz, double *work, int *lwork,
+                          int *iwork, int *ifail, int *info);
+extern void scipy_dgemm_(char *ta, char *tb, int *m, int *n, int *k, double *alpha,
+                         double *a, int *lda, double *b, int *ldb, double *beta,
+                         double *c, int *ldc);
+extern void scipy_dsymm_(char *side, char *uplo, int *m, int *n, double *alpha, double *a,
+                         int *lda, double *b, int *ldb, double *beta, double *c, int *ldc);
+extern double scipy_ddot_(int *n, double *x, int *incx, double *y, int *incy);
+extern double scipy_dnrm2_(int *n, double *x, int *incx);
+extern void scipy_dscal_(int *n, double *a, double *x, int *incx);
+
+static double arr_dot(double *x, double *y, int n) { int one = 1; return scipy_ddot_(&n, x, &one, y, &one); }
+static double arr_nrm2(double *x, int n) { int one = 1; return scipy_dnrm2_(&n, x, &one); }
+static void arr_scal(double a, double *x, int n) { int one = 1; scipy_dscal_(&n, &a, x, &one); }
+static void dgemm(char ta, char tb, int m, int n, int k, double alpha, double *a, int lda,
+                  double *b, int ldb, double beta, double *c, int ldc)
+{
+    scipy_dgemm_(&ta, &tb, &m, &n, &k, &alpha, a, &lda, b, &ldb, &beta, c, &ldc);
+}
+
+/* --------------------------------------------------------------- CSR ops */
+typedef struct { int n; const int *rp, *ci; const double *v; } csr_t;
+
+/* app/csr/gcge_app_csr.c:297-323: zero y, then accumulate row by row */
+static void csr_mv(const csr_t *A, const double *x, double *y)
+{
+    memset(y, 0, (size_t)A->n * sizeof(double));
+    for (int i = 0; i < A->n; ++i)
+        for (int j = A->rp[i]; j < A->rp[i + 1]; ++j)
+            y[i] += A->v[j] * x[A->ci[j]];
+}
+
+/* app/csr/gcge_app_csr.c:330-365: y = a x + b y with its three special cases */
+static void vaxpby(int n, double a, const double *x, double b, double *y)
+{
+    if (a == 0.0) {
+        for (int i = 0; i < n; ++i) y[i] = b * y[i];
+    } else if (b == 0.0) {
+        if (a == 1.0) for (int i = 0; i < n; ++i) y[i] = x[i];
+        else          for (int i = 0; i < n; ++i) y[i] = a * x[i];
+    } else {
+        for (int i = 0; i < n; ++i) y[i] = a * x[i] + b * y[i];
+    }
+}
+
+/* app/csr/gcge_app_csr.c:368-378 */
+static double vdot(int n, const double *x, const double *y)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += x[i] * y[i];
+    return s;
+}
+
+/* counter hash shared with the GPU solver's initial vectors (splitmix64 finaliser) */
+double gcge_oracle_hash_uniform(unsigned long long seed, unsigned long long index)
+{
+    unsigned long long z = seed ^ (index * 0xD1B54A32D192ED03ULL);
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* ----------------------------------------------------------- multivector */
+/* An ordered set of columns; the reference's void** multivector. */
+typedef struct { int n, k; double **c; double *store; } mv_t;
+
+static void mv_alloc(mv_t *m, int n, int k)
+{
+    m->n = n; m->k = k;
+    m->store = (double *)calloc((size_t)n * (k > 0 ? k : 1), sizeof(double));
+    m->c = (double **)malloc(sizeof(double *) * (k > 0 ? k : 1));
+    for (int j = 0; j < k; ++j) m->c[j] = m->store + (size_t)j * n;
+}
+static void mv_free(mv_t *m) { free(m->store); free(m->c); m->store = NULL; m->c = NULL; }
+
+/* src/gcge_ops.c:115-129 */
+static void mv_matdot(const csr_t *A, mv_t *x, mv_t *y, const int *s, const int *e)
+{
+    for (int i = 0; i < e[0] - s[0]; ++i) csr_mv(A, x->c[s[0] + i], y->c[s[1] + i]);
+}
+/* src/gcge_ops.c:132-146 */
+static void mv_axpby(double a, mv_t *x, double b, mv_t *y, const int *s, const int *e)
+{
+    for (int i = 0; i < e[0] - s[0]; ++i) vaxpby(x->n, a, x->c[s[0] + i], b, y->c[s[1] + i]);
+}
+/* src/gcge_ops.c:163-193: first column by a*x + 0*y, the rest accumulated with b = 1 */
+static void mv_lincomb(mv_t *x, mv_t *y, const int *s, const int *e, const double *a, int lda)
+{
+    for (int jy = s[1]; jy < e[1]; ++jy) {
+        const double *col = a + (size_t)(jy - s[1]) * lda;
+        vaxpby(x->n, col[0], x->c[s[0]], 0.0, y->c[jy]);
+        for (int ix = s[0] + 1; ix < e[0]; ++ix)
+            vaxpby(x->n, col[ix - s[0]], x->c[ix], 1.0, y->c[jy]);
+    }
+}
+/* src/gcge_ops.c:198-261 (MPI reduction omitted: one process) */
+static void mv_inner(mv_t *V, mv_t *W, double *a, int sym, const int *s, const int *e, int lda)
+{
+    if (sym) {
+        int len = e[1] - s[1];
+        double *p = a;
+        for (int iw = 0; iw < len; ++iw) {
+            for (int iv = 0; iv <= iw; ++iv, ++p)
+                *p = vdot(V->n, V->c[iv + s[0]], W->c[iw + s[1]]);
+            p += lda - (iw + 1);
+        }
+        for (int iw = 0; iw < len; ++iw)
+            for (int iv = iw + 1; iv < len; ++iv)
+                a[(size_t)iw * lda + iv] = a[(size_t)iv * lda + iw];
+    } else {
+        int skip = lda - (e[0] - s[0]);
+        double *p = a;
+        for (int iw = s[1]; iw < e[1]; ++iw) {
+            for (int iv = s[0]; iv < e[0]; ++iv, ++p)
+                *p = vdot(V->n, V->c[iv], W->c[iw]);
+            p += skip;
+        }
+    }
+}
+/* src/gcge_ops.c:285-300: exchange column pointers */
+static void mv_swap(mv_t *a, mv_t *b, const int *s, const int *e)
+{
+    for (int i = 0; i < e[0] - s[0]; ++i) {
+        double *t = a->c[s[0] + i];
+        a->c[s[0] + i] = b->c[s[1] + i];
+        b->c[s[1] + i] = t;
+    }
+}
+
+/* ------------------------------------------------------------------ state */
+typedef struct {
+    /* parameters (after GCGE_PARA_Setup, src/gcge_para.c:357-386) */
+    int nev, block_size, ev_max_it, cg_max_it, max_reorth_time, dirichlet, print_level;
+    double ev_tol, cg_rate, orth_zero_tol, reorth_tol, scbgs_reorth_tol, criterion_tol;
+    double multi_tol_for_lock, conv_omega_norm;
+    char conv_type[4];
+    /* para outputs */
+    int num_unlock, num_iter;
+    double max_res, min_res, sum_res;
+    double *res;
+    /* workspace (src/gcge_workspace.c:61-119) */
+    int max_dim_x, dim_x, dim_xp, dim_xpw, last_dim_xpw, last_dim_x, unconv_bs, soft_locked;
+    mv_t V, V_tmp, CG_p, evec;
+    int *unlock;
+    double *eval, *sub_dtmp, *sub_evec, *sub_mat;
+    int *sub_itmp;
+    const csr_t *A, *B;
+} gcge_t;
+
+/* ------------------------------------------------------- block CG (a8) */
+/* GCGE_BCG, src/gcge_cg.c:137-302. CG_R = RHS, CG_P = p-block, CG_W = w-block,
+ * CG_X = X[:, xs : xs+len]. The active list is rebuilt each iteration by writing
+ * unlock[idx] = idx at position idx (src/gcge_cg.c:713-720), so the update loops,
+ * which walk unlock[0 .. num_unlock), always touch the first num_unlock columns. */
+static void bcg(const csr_t *A, mv_t *R, mv_t *X, int xs, int len, mv_t *P, mv_t *Wk,
+                double *dtmp, int *itmp, int cg_max_it, double rate)
+{
+    int n = A->n;
+    double *rho1 = dtmp, *rho2 = rho1 + len, *err = rho2 + len, *lerr = err + len, *ptw = lerr + len;
+    int *unlock = itmp, num_unlock = 0;
+    for (int idx = 0; idx < len; ++idx) {
+        csr_mv(A, X->c[xs + idx], Wk->c[idx]);
+        vaxpby(n, -1.0, Wk->c[idx], 1.0, R->c[idx]);
+        rho2[idx] = vdot(n, R->c[idx], R->c[idx]);
+        unlock[idx] = idx;
+        num_unlock++;
+    }
+    for (int idx = 0; idx < len; ++idx) err[idx] = sqrt(rho2[idx]);
+    int niter = 1;
+    while (num_unlock > 0 && niter < cg_max_it) {
+        if (niter == 1) {
+            for (int id = 0; id < num_unlock; ++id) {
+                int idx = unlock[id];
+                vaxpby(n, 1.0, R->c[idx], 0.0, P->c[idx]);
+            }
+        } else {
+            for (int id = 0; id < num_unlock; ++id) {
+                int idx = unlock[id];
+                double beta = rho2[idx] / rho1[idx];
+                vaxpby(n, 1.0, R->c[idx], beta, P->c[idx]);
+            }
+        }
+        for (int id = 0; id < num_unlock; ++id) {
+            int idx = unlock[id];
+            csr_mv(A, P->c[idx], Wk->c[idx]);
+            ptw[idx] = vdot(n, P->c[idx], Wk->c[idx]);
+        }
+        for (int id = 0; id < num_unlock; ++id) {
+            int idx = unlock[id];
+            double alpha = rho2[idx] / ptw[idx];
+            vaxpby(n, alpha, P->c[idx], 1.0, X->c[xs + idx]);
+            vaxpby(n, -alpha, Wk->c[idx], 1.0, R->c[idx]);
+            rho1[idx] = rho2[idx];
+            rho2[idx] = vdot(n, R->c[idx], R->c[idx]);
+        }
+        for (int idx = 0; idx < len; ++idx) lerr[idx] = sqrt(fabs(rho2[idx]));
+        num_unlock = 0;
+        for (int idx = 0; idx < len; ++idx)
+            if (lerr[idx] / err[idx] >= rate) { unlock[idx] = idx; num_unlock++; }
+        niter++;
+    }
+}
+
+/* ------------------------------------------------ orthogonalisation (a10/a11) */
+/* GCGE_Orthonormalization, src/gcge_orthogonal.c:112-305: vector-by-vector
+ * B-orthonormalisation with re-orthogonalisation; the column (MGS) form is used when
+ * 0 < sum_res < criterion_tol, the block (CGS) form otherwise. Returns the new end. */
+static int orth_plain(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    int n = V->n;
+    double *d = g->sub_dtmp;
+    double vin = 0.0, vout = 0.0, ratio;
+    double *t0 = g->V_tmp.c[0], *t1 = g->V_tmp.c[1];
+    for (int cur = start; cur < end; ++cur) {
+        int reorth = 0;
+        if (g->sum_res > 0.0 && g->sum_res < g->criterion_tol) {
+            double *vc = V->c[cur];
+            if (!B) vout = sqrt(vdot(n, vc, vc));
+            else { csr_mv(B, vc, t1); vout = sqrt(vdot(n, vc, t1)); }
+            do {
+                for (int j = 0; j < cur; ++j) {
+                    double ipv;
+                    if (!B) ipv = vdot(n, vc, V->c[j]);
+                    else { csr_mv(B, vc, t1); ipv = vdot(n, V->c[j], t1); }
+                    vaxpby(n, -ipv, V->c[j], 1.0, vc);
+                }
+                vin = vout;
+                double nv;
+                if (!B) nv = vdot(n, vc, vc);
+                else { csr_mv(B, vc, t1); nv = vdot(n, vc, t1); }
+                vout = sqrt(nv);
+                ratio = vout / vin;
+                /* the reference never advances its counter on this path
+                 * (src/gcge_orthogonal.c:207); the norm test ends the loop */
+            } while (ratio < g->reorth_tol && reorth < g->max_reorth_time && vout > g->orth_zero_tol);
+        } else {
+            do {
+                if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, t0);
+                else csr_mv(B, V->c[cur], t0);
+                int s[2] = {0, 0}, e[2] = {cur + 1, 1};
+                mv_inner(V, &g->V_tmp, d, 0, s, e, cur + 1);
+                if (cur != 0) {
+                    int s2[2] = {0, 0}, e2[2] = {cur, 1};
+                    mv_lincomb(V, &g->V_tmp, s2, e2, d, cur);
+                    vaxpby(n, -1.0, t0, 1.0, V->c[cur]);
+                }
+                vin = sqrt(d[cur]);
+                d[cur] = d[cur] - arr_dot(d, d, cur);
+                vout = sqrt(d[cur]);
+                ratio = vout / vin;
+                reorth++;
+            } while (ratio < g->reorth_tol && reorth < g->max_reorth_time && vout > g->orth_zero_tol);
+        }
+        if (vout > g->orth_zero_tol) {
+            vaxpby(n, 0.0, V->c[cur], 1.0 / vout, V->c[cur]);
+        } else {
+            int s[2] = {cur, end - 1}, e[2] = {cur + 1, end};
+            mv_swap(V, V, s, e);
+            end--;
+            cur--;
+        }
+    }
+    return end;
+}
+
+/* GCGE_SubOrthonormalization, src/gcge_orthogonal.c:1880-1929:
+ * V2 -= V1 (V1^T B V2), Gram left in sub_dtmp (len1 x len2, ld len1). */
+static void sub_orth(gcge_t *g, mv_t *V, const int *s, const int *e, const csr_t *B)
+{
+    int len1 = e[0] - s[0], len2 = e[1] - s[1];
+    int ms[2] = {s[1], 0}, me[2] = {e[1], len2};
+    if (!B) mv_axpby(1.0, V, 0.0, &g->V_tmp, ms, me);
+    else mv_matdot(B, V, &g->V_tmp, ms, me);
+    int is[2] = {s[0], 0}, ie[2] = {e[0], len2};
+    mv_inner(V, &g->V_tmp, g->sub_dtmp, 0, is, ie, len1);
+    mv_lincomb(V, &g->V_tmp, is, ie, g->sub_dtmp, len1);
+    int as[2] = {0, s[1]}, ae[2] = {len2, e[1]};
+    mv_axpby(-1.0, &g->V_tmp, 1.0, V, as, ae);
+}
+
+/* GCGE_SubOrthonormalizationSelfBGS, src/gcge_orthogonal.c:2035-2115 */
+static int self_bgs(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    int n = V->n;
+    double *d = g->sub_dtmp, *t0 = g->V_tmp.c[0];
+    for (int cur = start; cur < end; ++cur) {
+        if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, t0);
+        else csr_mv(B, V->c[cur], t0);
+        int s[2] = {cur, 0}, e[2] = {end, 1};
+        mv_inner(V, &g->V_tmp, d, 0, s, e, end - cur);
+        double nrm = sqrt(d[0]);
+        if (nrm > g->orth_zero_tol) {
+            vaxpby(n, 0.0, V->c[cur], 1.0 / nrm, V->c[cur]);
+            for (int j = cur + 1; j < end; ++j)
+                vaxpby(n, -d[j - cur] / nrm, V->c[cur], 1.0, V->c[j]);
+        } else {
+            int s2[2] = {cur, end - 1}, e2[2] = {cur + 1, end};
+            mv_swap(V, V, s2, e2);
+            end--;
+            cur--;
+        }
+    }
+    return end;
+}
+
+/* GCGE_MultiOrthonormalization, src/gcge_orthogonal.c:1945-2033: recursive
+ * bisection; leaves (length <= max_direct_orth_length = 1) go to SelfBGS. */
+static int multi_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    int length = end - start;
+    int l1 = length / 2, l2 = length - l1, mid = start + l1;
+    if (length <= 1) return self_bgs(g, V, start, end, B);
+    mid = multi_orth(g, V, start, mid, B);
+    if (mid + l2 < end) {
+        int new_end_2 = mid + l2, n_zero = end - new_end_2;
+        int s[2] = {mid, new_end_2}, e[2] = {mid + n_zero, end};
+        mv_swap(V, V, s, e);
+        end = new_end_2;
+    }
+    if (mid - start > 0) {
+        double value_inner = 1.0;
+        int iter = 0;
+        while (value_inner > g->scbgs_reorth_tol) {
+            iter++;
+            int s[2] = {start, mid}, e[2] = {mid, end};
+            sub_orth(g, V, s, e, B);
+            value_inner = 0.0;
+            for (int i = 0; i < l1 * l2; ++i) value_inner += g->sub_dtmp[i] * g->sub_dtmp[i];
+            value_inner = sqrt(value_inner);
+            if (iter >= g->max_reorth_time) break;
+        }
+    }
+    return multi_orth(g, V, mid, end, B);
+}
+
+/* GCGE_StableMultiOrthonormalization, src/gcge_orthogonal.c:1833-1877 */
+static int stable_multi_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    double value_inner = 1.0;
+    int iter = 0;
+    while (value_inner > g->scbgs_reorth_tol) {
+        iter++;
+        int s[2] = {0, start}, e[2] = {start, end};
+        sub_orth(g, V, s, e, B);
+        value_inner = 0.0;
+        for (int i = 0; i < start * (end - start); ++i) value_inner += g->sub_dtmp[i] * g->sub_dtmp[i];
+        value_inner = sqrt(value_inner);
+        if (iter >= g->max_reorth_time) break;
+    }
+    return multi_orth(g, V, start, end, B);
+}
+
+/* GCGE_MultiOrthonormalizationInSubspace, src/gcge_orthogonal.c:2130-2204 (B = I) */
+static int multi_orth_sub(gcge_t *g, double *V, int ldV, int nrows, int start, int end)
+{
+    int length = end - start;
+    int l1 = length / 2, l2 = length - l1, mid = start + l1;
+    if (length == 1) {
+        double nv = arr_nrm2(V + (size_t)start * ldV, nrows);
+        if (nv > g->orth_zero_tol) arr_scal(1.0 / nv, V + (size_t)start * ldV, nrows);
+        else end = start;
+        return end;
+    }
+    mid = multi_orth_sub(g, V, ldV, nrows, start, mid);
+    if (mid + l2 < end) {
+        int new_end_2 = mid + l2, n_zero = end - new_end_2;
+        l1 -= n_zero;
+        memcpy(V + (size_t)mid * ldV, V + (size_t)new_end_2 * ldV, (size_t)n_zero * ldV * sizeof(double));
+        end = new_end_2;
+    }
+    if (l1 > 0) {
+        for (int r = 0; r < g->max_reorth_time; ++r) {
+            dgemm('T', 'N', l1, l2, nrows, 1.0, V + (size_t)start * ldV, ldV,
+                  V + (size_t)mid * ldV, ldV, 0.0, g->sub_dtmp, l1);
+            dgemm('N', 'N', ldV, l2, l1, -1.0, V + (size_t)start * ldV, ldV,
+                  g->sub_dtmp, l1, 1.0, V + (size_t)mid * ldV, ldV);
+        }
+    }
+    return multi_orth_sub(g, V, ldV, nrows, mid, end);
+}
+
+/* GCGE_StableMultiOrthonormalizationInSubspace, src/gcge_orthogonal.c:2215-2247 */
+static int stable_multi_orth_sub(gcge_t *g, double *V, int ldV, int nrows, int start, int end)
+{
+    if (start != 0) {
+        for (int r = 0; r < g->max_reorth_time; ++r) {
+            int len = end - start;
+            dgemm('T', 'N', start, len, nrows, 1.0, V, ldV, V + (size_t)start * ldV, ldV,
+                  0.0, g->sub_dtmp, start);
+            dgemm('N', 'N', ldV, len, start, -1.0, V, ldV, g->sub_dtmp, start, 1.0,
+                  V + (size_t)start * ldV, ldV);
+        }
+    }
+    return multi_orth_sub(g, V, ldV, nrows, start, end);
+}
+
+/* ----------------------------------------------------- Rayleigh-Ritz (a16/a17) */
+/* GCGE_ComputeSubspaceMatrixVTAW, src/gcge_rayleighritz.c:35-81 */
+static void rr_vtaw(gcge_t *g, const csr_t *A, int start_W, int end_V, double *sub)
+{
+    int w_len = end_V - start_W, xp_len = end_V - w_len;
+    int s[2] = {start_W, 0}, e[2] = {end_V, w_len};
+    mv_matdot(A, &g->V, &g->evec, s, e);
+    int s2[2] = {0, 0}, e2[2] = {xp_len, w_len};
+    mv_inner(&g->V, &g->evec, sub, 0, s2, e2, end_V);
+    mv_inner(&g->V, &g->evec, sub + xp_len, 1, s, e, end_V);
+}
+
+/* GCGE_ComputeSubspaceMatrix, src/gcge_rayleighritz.c:113-200 (structured form) */
+static void rr_matrix(gcge_t *g, const csr_t *A)
+{
+    int dim_xp = g->dim_xp, ldm = g->dim_xpw;
+    if (dim_xp != 0) {
+        int lde = g->last_dim_xpw, dim_x = g->dim_x, dim_p = dim_xp - dim_x;
+        double one = 1.0, zero = 0.0;
+        double *pp = g->sub_evec + (size_t)dim_x * lde;
+        char L = 'L', U = 'U';
+        scipy_dsymm_(&L, &U, &lde, &dim_p, &one, g->sub_mat, &lde, pp, &lde, &zero, g->sub_dtmp, &lde);
+        memset(g->sub_mat, 0, (size_t)ldm * ldm * sizeof(double));
+        dgemm('T', 'N', dim_p, dim_p, lde, 1.0, pp, lde, g->sub_dtmp, lde, 0.0,
+              g->sub_mat + (size_t)dim_x * ldm + dim_x, ldm);
+        for (int i = 0; i < dim_x; ++i) g->sub_mat[(size_t)i * ldm + i] = g->eval[i];
+    }
+    rr_vtaw(g, A, dim_xp, ldm, g->sub_mat + (size_t)dim_xp * ldm);
+}
+
+/* GCGE_ComputeSubspaceEigenpairs, src/gcge_rayleighritz.c:364-590, single-process
+ * path with opt_rr_eig_partly = 0 (so rr_eigen_start = 0): dsyevx("V","I","U")
+ * for eigenpairs 1 .. min(max_dim_x, ldm) of a copy of the projected matrix. */
+static int rr_eig(gcge_t *g)
+{
+    int ldm = g->dim_xpw;
+    double *tmp = g->sub_dtmp, *work = tmp + (size_t)ldm * ldm;
+    double vl = 0.0, vu = 0.0, abstol = 0.0;
+    int il = 1, iu = g->max_dim_x < ldm ? g->max_dim_x : ldm, m = iu - il + 1;
+    int lwork = 8 * ldm, info = 0, nrows = ldm, ncols = ldm;
+    int *iwork = g->sub_itmp, *ifail = g->sub_itmp + 5 * ldm;
+    g->soft_locked = 0;
+    memcpy(tmp, g->sub_mat, (size_t)ldm * ldm * sizeof(double));
+    char V = 'V', I = 'I', U = 'U';
+    scipy_dsyevx_(&V, &I, &U, &nrows, tmp, &ncols, &vl, &vu, &il, &iu, &abstol, &m,
+                  g->eval, g->sub_evec, &ldm, work, &lwork, iwork, ifail, &info);
+    return info;
+}
+
+/* -------------------------------------------------------- X, P, W (a9/a14/a15) */
+/* GCGE_ComputeX, src/gcge_xpw.c:47-76 */
+static void compute_x(gcge_t *g, int size_x, int size_v)
+{
+    int sx = g->soft_locked;
+    int s[2] = {sx, sx}, e[2] = {size_v, size_x};
+    mv_lincomb(&g->V, &g->evec, s, e, g->sub_evec + (size_t)sx * size_v + sx, size_v);
+}
+
+/* GCGE_ComputeW, src/gcge_xpw.c:118-217 (built-in block CG, no external solver) */
+static void compute_w(gcge_t *g, const csr_t *A, const csr_t *B)
+{
+    int n = A->n, ws = g->dim_xp, wl = g->unconv_bs;
+    for (int idx = 0; idx < wl; ++idx) {
+        double *rhs = g->V_tmp.c[idx];
+        int xi = g->unlock[idx];
+        double *x = g->V.c[xi], *w = g->V.c[ws + idx];
+        if (!B) vaxpby(n, 1.0, x, 0.0, rhs);
+        else csr_mv(B, x, rhs);
+        double lam = g->eval[xi];
+        if (fabs(lam) <= 1.0) {
+            vaxpby(n, 0.0, rhs, lam, rhs);
+            vaxpby(n, 1.0, x, 0.0, w);
+        } else {
+            vaxpby(n, 1.0 / lam, x, 0.0, w);
+        }
+    }
+    bcg(A, &g->V_tmp, &g->V, ws, wl, &g->CG_p, &g->evec, g->sub_dtmp, g->sub_itmp,
+        g->cg_max_it, g->cg_rate);
+}
+
+/* GCGE_ComputeP, src/gcge_xpw.c:286-425 */
+static void compute_p(gcge_t *g)
+{
+    double *coef = g->sub_evec;
+    int ldc = g->dim_xpw, p_start = g->dim_x, p_ncols = g->unconv_bs, xx_nrows = g->last_dim_x;
+    double *px = coef + (size_t)p_start * ldc, *pp = px + xx_nrows, *xp = coef + xx_nrows;
+    memset(px, 0, (size_t)p_ncols * ldc * sizeof(double));
+    for (int cp = 0; cp < p_ncols; ++cp)
+        memcpy(pp + (size_t)cp * ldc, xp + (size_t)g->unlock[cp] * ldc,
+               (size_t)(ldc - xx_nrows) * sizeof(double));
+    int orth_start = g->soft_locked, orth_len = ldc - orth_start;
+    p_start -= orth_start;
+    int p_end = p_start + p_ncols;
+    p_end = stable_multi_orth_sub(g, coef + (size_t)orth_start * ldc + orth_start, ldc, orth_len,
+                                  p_start, p_end);
+    p_end += orth_start;
+    int p_end_tmp = p_end - g->nev;
+    int s[2] = {orth_start, 0}, e[2] = {ldc, p_end_tmp};
+    mv_lincomb(&g->V, &g->V_tmp, s, e, coef + (size_t)g->nev * ldc + orth_start, ldc);
+    int s2[2] = {g->nev, 0}, e2[2] = {p_end, p_end_tmp};
+    mv_swap(&g->V, &g->V_tmp, s2, e2);
+    g->dim_xp = p_end;
+}
+
+/* ------------------------------------------------------ convergence (a18/a19) */
+/* GCGE_CheckConvergence, src/gcge_eigsol.c:559-686, plus the "BR" criterion */
+static void check_conv(gcge_t *g, const csr_t *A, const csr_t *B)
+{
+    int n = A->n, unconv = 0, max_conv_idx = 0, num_unlock = g->num_unlock;
+    double max_res = 0.0, min_res = 0.0, sum_res = 0.0;
+    double *t1 = g->V_tmp.c[0], *t2 = g->V_tmp.c[1];
+    for (int j = 0; j < num_unlock; ++j) {
+        int i = g->unlock[j];
+        double *ev = g->evec.c[i], lam = g->eval[i], bxn = 0.0;
+        csr_mv(A, ev, t1);
+        if (!B) { vaxpby(n, -lam, ev, 1.0, t1); }
+        else { csr_mv(B, ev, t2); vaxpby(n, -lam, t2, 1.0, t1); }
+        double rn = sqrt(vdot(n, t1, t1));
+        double en = sqrt(vdot(n, ev, ev));
+        double r;
+        if (strcmp(g->conv_type, "R") == 0) r = rn / en / (1.0 > fabs(lam) ? 1.0 : fabs(lam));
+        else if (strcmp(g->conv_type, "O") == 0) r = rn / en / (g->conv_omega_norm + fabs(lam));
+        else if (strcmp(g->conv_type, "BR") == 0) {
+            bxn = B ? sqrt(vdot(n, t2, t2)) : en;
+            r = rn / (fabs(lam) * bxn);
+        } else r = rn / en;
+        g->res[i] = r;
+        sum_res += r;
+        if (j == 0) { max_res = r; min_res = r; }
+        else { if (r > max_res) max_res = r; if (r < min_res) min_res = r; }
+        if (r > g->ev_tol) {
+            g->unlock[unconv++] = i;
+            if (j > max_conv_idx + 8) {
+                for (int k = j + 1; k < num_unlock; ++k) g->unlock[unconv++] = g->unlock[k];
+                j = num_unlock + 1;
+            }
+        } else {
+            max_conv_idx = j;
+        }
+    }
+    g->num_unlock = unconv;
+    g->unconv_bs = unconv < g->block_size ? unconv : g->block_size;
+    g->max_res = max_res; g->min_res = min_res; g->sum_res = sum_res;
+    g->num_iter += 1;
+    if (g->print_level > 0)
+        printf("num_unlock(%3d) = %3d; max_res(%3d) = %e; min_res(%3d) = %e;\n",
+               g->num_iter, g->num_unlock, g->num_iter, max_res, g->num_iter, min_res);
+}
+
+/* GCGE_CheckEvalMultiplicity, src/gcge_eigsol.c:696-718 */
+static int check_multiplicity(int nev, int end, const double *eval)
+{
+    int t = nev;
+    for (int i = nev; i < end; ++i) {
+        if (fabs(fabs(eval[t] / eval[nev]) - 1) < 0.2) t += 1;
+        else break;
+    }
+    return t;
+}
+
+/* CSR_SetDirichletBoundary, app/csr/gcge_app_csr.c:130-183 */
+static void dirichlet_zero(gcge_t *g, const csr_t *A, const csr_t *B)
+{
+    if (!A || !B) return;
+    for (int i = 0; i < A->n; ++i) {
+        int zero_b = 1;
+        for (int j = B->rp[i]; j < B->rp[i + 1]; ++j)
+            if (fabs(B->v[j]) > 1e-20) { zero_b = 0; break; }
+        if (!zero_b) continue;
+        int cnt = 0;
+        for (int j = A->rp[i]; j < A->rp[i + 1]; ++j)
+            if (fabs(A->v[j]) > 1e-20) cnt++;
+        if (cnt == 1)
+            for (int k = 0; k < g->nev; ++k) g->evec.c[k][i] = 0.0;
+    }
+}
+
+/* ------------------------------------------------------------------ solve */
+void gcge_oracle_default_params(gcge_oracle_params *p)
+{
+    memset(p, 0, sizeof(*p));
+    p->nev = 1; p->block_size = 0; p->ev_max_it = 30; p->cg_max_it = 20; p->max_reorth_time = 3;
+    p->ev_tol = 1e-8; p->cg_rate = 1e-2; p->orth_zero_tol = 1e-16; p->reorth_tol = 0.75;
+    p->scbgs_reorth_tol = 1e-16; p->criterion_tol = 1e-6;
+    strcpy(p->conv_type, "R");
+    p->init_rng = 0; p->seed = 1;
+}
+
+static void random_columns(gcge_t *g, const gcge_oracle_params *p, int from, int count)
+{
+    int n = g->evec.n;
+    for (int j = from; j < from + count; ++j) {
+        double *c = g->evec.c[j];
+        if (p->init_rng == 0) {
+            for (int i = 0; i < n; ++i) c[i] = ((double)rand()) / ((double)RAND_MAX + 1);
+        } else {
+            for (int i = 0; i < n; ++i)
+                c[i] = gcge_oracle_hash_uniform(p->seed, (unsigned long long)j * n + i);
+        }
+    }
+}
+
+int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v,
+                      const int *B_rp, const int *B_ci, const double *B_v,
+                      const gcge_oracle_params *p, double *eval_out, double *evec_out,
+                      gcge_oracle_stats *st)
+{
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    csr_t Am = {n, A_rp, A_ci, A_v}, Bm = {n, B_rp, B_ci, B_v};
+    const csr_t *A = &Am, *B = B_rp ? &Bm : NULL;
+    gcge_t G, *g = &G;
+    memset(g, 0, sizeof(G));
+    g->A = A; g->B = B;
+    /* GCGE_PARA_Setup, src/gcge_para.c:357-386 */
+    int nev = p->nev;
+    g->nev = nev;
+    g->block_size = p->block_size ? p->block_size : nev;
+    g->ev_max_it = p->ev_max_it; g->cg_max_it = p->cg_max_it; g->max_reorth_time = p->max_reorth_time;
+    g->dirichlet = p->dirichlet_boundary; g->print_level = p->print_level;
+    g->ev_tol = p->ev_tol; g->cg_rate = p->cg_rate;
+    g->orth_zero_tol = p->orth_zero_tol + DBL_EPSILON;
+    g->reorth_tol = p->reorth_tol;
+    g->scbgs_reorth_tol = p->scbgs_reorth_tol + DBL_EPSILON;
+    g->criterion_tol = p->criterion_tol;
+    strncpy(g->conv_type, p->conv_type, 3);
+    g->num_unlock = nev;
+    g->res = (double *)malloc(sizeof(double) * nev);
+    for (int i = 0; i < nev; ++i) g->res[i] = 1.0;
+    /* GCGE_WORKSPACE_Setup, src/gcge_workspace.c:61-119 */
+    int mtmp = (nev * 1.25 < nev + 8) ? (int)(nev * 1.25) : (nev + 8);
+    int max_dim_x = mtmp > nev + 3 ? mtmp : nev + 3;
+    int bs = g->block_size;
+    int V_size = max_dim_x + 2 * bs, Vt_size = max_dim_x - nev + bs, max_dim_xpw = V_size;
+    mv_alloc(&g->V, n, V_size);
+    mv_alloc(&g->V_tmp, n, Vt_size);
+    mv_alloc(&g->CG_p, n, bs);
+    mv_alloc(&g->evec, n, nev);
+    g->max_dim_x = max_dim_x; g->dim_x = nev; g->dim_xp = 0; g->dim_xpw = nev;
+    g->unconv_bs = nev < bs ? nev : bs;
+    g->eval = (double *)calloc(max_dim_xpw, sizeof(double));
+    g->sub_dtmp = (double *)calloc((size_t)max_dim_xpw * max_dim_xpw + 40 * (size_t)max_dim_xpw, sizeof(double));
+    g->sub_itmp = (int *)calloc(100 * (size_t)max_dim_xpw, sizeof(int));
+    g->sub_evec = (double *)calloc((size_t)max_dim_xpw * max_dim_xpw, sizeof(double));
+    g->sub_mat = (double *)calloc((size_t)max_dim_xpw * max_dim_xpw, sizeof(double));
+    g->unlock = (int *)calloc(max_dim_x, sizeof(int));
+    for (int i = 0; i < max_dim_x; ++i) g->unlock[i] = i;
+
+    if (p->init_rng == 0) srand((unsigned)p->seed);
+    int status = 0;
+
+    /* initial X, src/gcge_eigsol.c:126-207 */
+    if (p->given_init_evec == 0) {
+        int num_init = 0;
+        int guard = 0;
+        do {
+            random_columns(g, p, num_init, nev - num_init);
+            if (strcmp(g->conv_type, "O") == 0 && num_init == 0) {
+                double omega = 0.0, aomega = 0.0;
+                for (int i = 0; i < nev; ++i) {
+                    double nv = vdot(n, g->evec.c[i], g->evec.c[i]);
+                    vaxpby(n, 0.0, g->evec.c[i], 1.0 / sqrt(nv), g->evec.c[i]);
+                }
+                for (int i = 0; i < nev; ++i) omega += vdot(n, g->evec.c[i], g->evec.c[i]);
+                int s[2] = {0, 0}, e[2] = {nev, nev};
+                mv_matdot(A, &g->evec, &g->V, s, e);
+                for (int i = 0; i < nev; ++i) aomega += vdot(n, g->V.c[i], g->V.c[i]);
+                g->conv_omega_norm = sqrt(aomega / omega);
+            }
+            if (g->dirichlet) dirichlet_zero(g, A, B);
+            g->dim_x = nev;
+            g->dim_x = orth_plain(g, &g->evec, num_init, g->dim_x, B);
+            num_init = g->dim_x;
+            if (++guard > 100) { status = 2; break; }
+        } while (num_init < nev);
+    } else {
+        for (int j = 0; j < nev; ++j) memcpy(g->evec.c[j], evec_out + (size_t)j * n, sizeof(double) * n);
+        g->dim_x = orth_plain(g, &g->evec, 0, nev, B);
+    }
+    {
+        int s[2] = {0, 0}, e[2] = {nev, nev};
+        mv_axpby(1.0, &g->evec, 0.0, &g->V, s, e);
+    }
+    g->dim_xpw = g->dim_x;
+    g->last_dim_x = g->dim_x;
+    g->dim_xp = 0;
+    rr_matrix(g, A);
+    if (rr_eig(g)) status = 3;
+    compute_x(g, nev, g->dim_xpw);
+    check_conv(g, A, B);
+    {
+        int s[2] = {g->soft_locked, g->soft_locked}, e[2] = {nev, nev};
+        mv_swap(&g->V, &g->evec, s, e);
+    }
+    g->dim_xp = g->dim_x;
+    compute_w(g, A, B);
+    g->last_dim_xpw = g->dim_xpw;
+    g->dim_xpw = g->dim_xp + g->unconv_bs;
+    g->dim_xpw = orth_plain(g, &g->V, g->dim_x, g->dim_xpw, B);
+    g->dim_xp = nev;
+    rr_matrix(g, A);
+    if (rr_eig(g)) status = 3;
+    compute_x(g, nev, g->dim_xpw);
+    check_conv(g, A, B);
+
+    /* main loop, src/gcge_eigsol.c:396-528 */
+    while (g->num_unlock > 0 && g->num_iter < g->ev_max_it) {
+        compute_p(g);
+        {
+            int s[2] = {g->soft_locked, g->soft_locked}, e[2] = {nev, nev};
+            mv_swap(&g->V, &g->evec, s, e);
+        }
+        compute_w(g, A, B);
+        g->last_dim_xpw = g->dim_xpw;
+        g->dim_xpw = g->dim_xp + g->unconv_bs;
+        g->dim_xpw = stable_multi_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
+        rr_matrix(g, A);
+        if (rr_eig(g)) status = 3;
+        g->last_dim_x = g->dim_x;
+        g->dim_x = check_multiplicity(nev, max_dim_x, g->eval);
+        compute_x(g, nev, g->dim_xpw);
+        check_conv(g, A, B);
+    }
+
+    memcpy(eval_out, g->eval, sizeof(double) * nev);
+    for (int j = 0; j < nev; ++j) memcpy(evec_out + (size_t)j * n, g->evec.c[j], sizeof(double) * n);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if (st) {
+        st->num_iter = g->num_iter; st->num_unlock = g->num_unlock;
+        st->max_res = g->max_res; st->min_res = g->min_res; st->sum_res = g->sum_res;
+        st->wall_s = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+        st->status = status;
+    }
+    mv_free(&g->V); mv_free(&g->V_tmp); mv_free(&g->CG_p); mv_free(&g->evec);
+    free(g->eval); free(g->sub_dtmp); free(g->sub_itmp); free(g->sub_evec); free(g->sub_mat);
+    free(g->unlock); free(g->res);
+    return status;
+}
+
+/* --------------------------------------------------------- single-op entries */
+void gcge_oracle_csr_matvec(int n, const int *rp, const int *ci, const double *v,
+                            const double *x, double *y)
+{
+    csr_t A = {n, rp, ci, v};
+    csr_mv(&A, x, y);
+}
+
+void gcge_oracle_csr_matmultivec(int n, int k, const int *rp, const int *ci, const double *v,
+                                 const double *X, double *Y)
+{
+    csr_t A = {n, rp, ci, v};
+    for (int j = 0; j < k; ++j) csr_mv(&A, X + (size_t)j * n, Y + (size_t)j * n);
+}
+
+void gcge_oracle_vec_axpby(int n, double a, const double *x, double b, double *y)
+{
+    vaxpby(n, a, x, b, y);
+}
+
+static void wrap_cols(mv_t *m, int n, int k, double *base)
+{
+    m->n = n; m->k = k; m->store = NULL;
+    m->c = (double **)malloc(sizeof(double *) * (k > 0 ? k : 1));
+    for (int j = 0; j < k; ++j) m->c[j] = base + (size_t)j * n;
+}
+
+void gcge_oracle_multivec_lincomb(int n, int nx, int ny, const double *X, double *Y,
+                                  const double *coef, int lda)
+{
+    mv_t x, y;
+    wrap_cols(&x, n, nx, (double *)X);
+    wrap_cols(&y, n, ny, Y);
+    int s[2] = {0, 0}, e[2] = {nx, ny};
+    mv_lincomb(&x, &y, s, e, coef, lda);
+    free(x.c); free(y.c);
+}
+
+void gcge_oracle_multivec_innerprod(int n, int nv, int nw, const double *V, const double *W,
+                                    double *a, int lda, int sym)
+{
+    mv_t v, w;
+    wrap_cols(&v, n, nv, (double *)V);
+    wrap_cols(&w, n, nw, (double *)W);
+    int s[2] = {0, 0}, e[2] = {nv, nw};
+    mv_inner(&v, &w, a, sym, s, e, lda);
+    free(v.c); free(w.c);
+}
+
+void gcge_oracle_bcg(int n, int k, const int *rp, const int *ci, const double *v,
+                     double *RHS, double *W, int cg_max_it, double cg_rate)
+{
+    csr_t A = {n, rp, ci, v};
+    mv_t R, X, P, Wk;
+    wrap_cols(&R, n, k, RHS);
+    wrap_cols(&X, n, k, W);
+    mv_alloc(&P, n, k);
+    mv_alloc(&Wk, n, k);
+    double *dtmp = (double *)calloc(6 * (size_t)(k + 1), sizeof(double));
+    int *itmp = (int *)calloc(k + 1, sizeof(int));
+    bcg(&A, &R, &X, 0, k, &P, &Wk, dtmp, itmp, cg_max_it, cg_rate);
+    free(dtmp); free(itmp); mv_free(&P); mv_free(&Wk); free(R.c); free(X.c);
+}
+
+int gcge_oracle_stable_multi_orth(int n, int ncols, double *Vd, int start, int end,
+                                  const int *B_rp, const int *B_ci, const double *B_v,
+                                  int max_reorth_time, double orth_zero_tol, double scbgs_reorth_tol)
+{
+    csr_t Bm = {n, B_rp, B_ci, B_v};
+    gcge_t G;
+    memset(&G, 0, sizeof(G));
+    G.max_reorth_time = max_reorth_time;
+    G.orth_zero_tol = orth_zero_tol + DBL_EPSILON;
+    G.scbgs_reorth_tol = scbgs_reorth_tol + DBL_EPSILON;
+    mv_t V;
+    wrap_cols(&V, n, ncols, Vd);
+    int width = end - start > 1 ? end - start : 1;
+    mv_alloc(&G.V_tmp, n, width);
+    G.sub_dtmp = (double *)calloc((size_t)(ncols + 1) * (ncols + 1) + 64, sizeof(double));
+    /* the column pointers may be permuted by zero-vector swaps: copy back in order */
+    int new_end = stable_multi_orth(&G, &V, start, end, B_rp ? &Bm : NULL);
+    double *tmp = (double *)malloc(sizeof(double) * (size_t)n * ncols);
+    for (int j = 0; j < ncols; ++j) memcpy(tmp + (size_t)j * n, V.c[j], sizeof(double) * n);
+    memcpy(Vd, tmp, sizeof(double) * (size_t)n * ncols);
+    free(tmp);
+    mv_free(&G.V_tmp);
+    free(G.sub_dtmp);
+    free(V.c);
+    return new_end;
+}

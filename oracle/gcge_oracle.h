@@ -1,0 +1,99 @@
+/*
+ * gcge_oracle.h -- CPU restatement of GCGE-1.0's CSR eigensolver path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle). Nothing in the product links this
+ * library; only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg load it, as the checker.
+ *
+ * Every function restates the reference algorithm step for step (same
+ * operation order, same parameter defaults, same quirks) so that, given the
+ * same initial vectors, its iterates agree with the compiled reference to
+ * rounding level. Citations are file:line inside the GCGE-1.0 project.
+ *
+ * Multivectors passed across this interface are column-major n x k arrays
+ * with leading dimension n.
+ */
+#ifndef GCGE_ORACLE_H
+#define GCGE_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Solver parameters; defaults follow GCGE_PARA_Create (src/gcge_para.c:25-99). */
+typedef struct {
+    int    nev;                 /* number of wanted eigenpairs                          */
+    int    block_size;          /* 0 -> nev (src/gcge_para.c:364-368)                   */
+    int    ev_max_it;           /* outer GCG iterations (default 30)                    */
+    int    cg_max_it;           /* block-CG iterations (default 20)                     */
+    int    max_reorth_time;     /* default 3                                            */
+    int    dirichlet_boundary;  /* zero Dirichlet rows of the initial X (csr app :130)  */
+    int    given_init_evec;     /* 1: evec holds the initial vectors on entry           */
+    double ev_tol;              /* default 1e-8                                         */
+    double cg_rate;             /* default 1e-2                                         */
+    double orth_zero_tol;       /* default 1e-16 (+DBL_EPSILON at setup)                */
+    double reorth_tol;          /* default 0.75                                         */
+    double scbgs_reorth_tol;    /* default 1e-16 (+DBL_EPSILON at setup)                */
+    double criterion_tol;       /* default 1e-6                                         */
+    char   conv_type[4];        /* "R" relative, "A" absolute, "O" omega-norm,
+                                   "BR": ||Ax - lambda Bx|| / (|lambda| ||Bx||)         */
+    int    init_rng;            /* 0: libc rand() after srand(seed) (the reference's),
+                                   1: counter-hash uniform [0,1) shared with the GPU    */
+    unsigned long long seed;
+    int    print_level;         /* 0 silent, 1 per-iteration line                       */
+} gcge_oracle_params;
+
+typedef struct {
+    int    num_iter;
+    int    num_unlock;
+    double max_res, min_res, sum_res;
+    double wall_s;              /* wall time of the solve (CLOCK_MONOTONIC)            */
+    int    status;              /* 0 ok                                                 */
+} gcge_oracle_stats;
+
+void gcge_oracle_default_params(gcge_oracle_params *p);
+
+/* Full GCGE solve, GCGE_Solve (src/gcge_eigsol.c:65-542) on the CSR backend.
+ * B may be NULL (B = I). eval[nev], evec[n*nev] (column-major) are outputs
+ * (evec is also the input when given_init_evec = 1). Returns 0 on success. */
+int gcge_oracle_solve(int n,
+                      const int *A_rp, const int *A_ci, const double *A_v,
+                      const int *B_rp, const int *B_ci, const double *B_v,
+                      const gcge_oracle_params *p,
+                      double *eval, double *evec, gcge_oracle_stats *st);
+
+/* ---- single operations, for per-kernel parity ---- */
+
+/* y = A x  (app/csr/gcge_app_csr.c:297-323) */
+void gcge_oracle_csr_matvec(int n, const int *rp, const int *ci, const double *v,
+                            const double *x, double *y);
+/* Y[:, j] = A X[:, j] for k columns (src/gcge_ops.c:115-129) */
+void gcge_oracle_csr_matmultivec(int n, int k, const int *rp, const int *ci, const double *v,
+                                 const double *X, double *Y);
+/* y = a x + b y with the backend's special cases (app/csr/gcge_app_csr.c:330-365) */
+void gcge_oracle_vec_axpby(int n, double a, const double *x, double b, double *y);
+/* Y[:, j] = sum_i X[:, i] * coef[j*lda + i]  (src/gcge_ops.c:163-193) */
+void gcge_oracle_multivec_lincomb(int n, int nx, int ny, const double *X, double *Y,
+                                  const double *coef, int lda);
+/* a = V^T W, "sym" fills the upper triangle and mirrors (src/gcge_ops.c:198-281) */
+void gcge_oracle_multivec_innerprod(int n, int nv, int nw, const double *V, const double *W,
+                                    double *a, int lda, int sym);
+/* Block CG on A W = RHS, GCGE_BCG (src/gcge_cg.c:137-302). RHS is overwritten by
+ * the residual, W (n x k) holds the initial guess on entry and the solution on exit. */
+void gcge_oracle_bcg(int n, int k, const int *rp, const int *ci, const double *v,
+                     double *RHS, double *W, int cg_max_it, double cg_rate);
+/* B-orthonormalise V[:, start:end) against V[:, 0:start) and itself with the default
+ * "multi" method, GCGE_StableMultiOrthonormalization (src/gcge_orthogonal.c:1833-1877).
+ * B may be NULL. Returns the new end (zero vectors are moved past it). */
+int gcge_oracle_stable_multi_orth(int n, int ncols, double *V, int start, int end,
+                                  const int *B_rp, const int *B_ci, const double *B_v,
+                                  int max_reorth_time, double orth_zero_tol, double scbgs_reorth_tol);
+
+/* Uniform [0,1) counter-hash value used for initial vectors when init_rng = 1;
+ * the GPU solver draws from the same function. */
+double gcge_oracle_hash_uniform(unsigned long long seed, unsigned long long index);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

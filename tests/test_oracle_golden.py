@@ -1,0 +1,96 @@
+"""The oracle (C restatement of GCGE-1.0's CSR path) against the reference.
+
+* golden.json holds what the compiled reference reported on each case; the oracle,
+  started from the same libc rand() stream, must reproduce it exactly
+  (same iteration count, eigenvalues to 1e-13 relative, eigenvector checksums).
+* Where the reference build exists (oracle/_ref), the two must agree bit for bit.
+* Known answers: analytic Laplacian and Q1-cube spectra.
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from gcge_gb300 import problems as P
+from _golden import case_matrices, golden
+
+G = golden()
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    return pyoracle.Oracle()
+
+
+@pytest.mark.parametrize("name", sorted(G))
+def test_oracle_matches_reference_golden(oracle, name):
+    g = G[name]
+    A, B = case_matrices(name)
+    assert A.n == g["n"] and A.nnz == g["nnz"]
+    ev, X, st = oracle.solve(A, B, oracle.params(**g["params"]))
+    assert st.num_iter == g["num_iter"]
+    assert st.num_unlock == g["num_unlock"]
+    np.testing.assert_allclose(ev, g["eval"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(X.sum(axis=0), g["evec_colsum"], rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(np.linalg.norm(X, axis=0), g["evec_colnorm"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["fem33_nev10_dirichlet", "laplace30x20_nev12_block4"])
+def test_oracle_bitwise_vs_reference_build(oracle, name):
+    ref = pyoracle.reference()
+    if ref is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    g = G[name]
+    A, B = case_matrices(name)
+    e1, X1, s1 = oracle.solve(A, B, oracle.params(**g["params"]))
+    e2, X2, s2 = ref.solve(A, B, ref.params(**g["params"]))
+    assert s1.num_iter == s2.num_iter
+    assert np.array_equal(e1, e2)
+    assert np.array_equal(X1, X2)
+
+
+def test_oracle_known_answer_laplace(oracle):
+    A, _ = P.laplace2d(100, 100)
+    ev, X, st = oracle.solve(A, None, oracle.params(nev=10, seed=3))
+    ex = P.laplace2d_eigs(100, 100, 10)
+    assert np.max(np.abs(ev - ex) / ex) < 1e-10
+
+
+def test_oracle_known_answer_femcube(oracle):
+    A, B = P.fem_q1_cube(12)
+    ev, X, st = oracle.solve(A, B, oracle.params(nev=8, seed=4, ev_max_it=100))
+    ex = P.fem_q1_cube_eigs(12, 8)
+    assert np.max(np.abs(ev - ex) / ex) < 1e-10
+
+
+def test_oracle_baseline_residual_criterion(oracle):
+    """conv_type "BR" stops on ||Ax - lambda Bx|| / (|lambda| ||Bx||) <= tol."""
+    A, B = P.fem_q1_cube(8)
+    ev, X, st = oracle.solve(A, B, oracle.params(nev=5, seed=9, conv_type="BR", ev_max_it=200))
+    As, Bs = A.to_scipy(), B.to_scipy()
+    for j in range(5):
+        r = As @ X[:, j] - ev[j] * (Bs @ X[:, j])
+        assert np.linalg.norm(r) / (abs(ev[j]) * np.linalg.norm(Bs @ X[:, j])) <= 1e-8
+
+
+def test_hash_rng_uniform(oracle):
+    v = np.array([oracle.hash_uniform(7, i) for i in range(20000)])
+    assert 0.0 <= v.min() and v.max() < 1.0
+    assert abs(v.mean() - 0.5) < 0.01
+
+
+def test_problem_generators_structure():
+    for A, B in (P.laplace2d(7, 5), P.fem_q1_cube(5), P.varcoef2d(9, seed=1), P.varcoef3d(6, seed=2)):
+        A.check()
+        assert np.allclose(A.to_scipy().toarray(), A.to_scipy().toarray().T)
+        if B is not None:
+            B.check()
+    A, B = P.powerlaw_graph(2000, seed=3, dmax=50)
+    A.check()
+    assert A.to_scipy().diagonal().min() > 0
+
+
+def test_fem_cube_analytic_eigs_match_dense():
+    import scipy.linalg as sl
+    A, B = P.fem_q1_cube(6)
+    w = sl.eigh(A.to_scipy().toarray(), B.to_scipy().toarray(), eigvals_only=True)[:10]
+    np.testing.assert_allclose(w, P.fem_q1_cube_eigs(6, 10), rtol=1e-12)
