@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Time to the nev smallest eigenpairs at residual <= 1e-8 with the GCGE CSR
+eigensolver on one GB300, mixed precision (FP32 inner block CG) against plain
+FP64, on the generalized Q1-FEM cube pencil.
+
+Workload (default "fem96"): Q1 trilinear stiffness A and consistent mass B on
+the unit cube with 96^3 elements, Dirichlet by elimination (n = 95^3 = 857,375,
+27-point stencils, nnz = 22,665,187 per matrix), the 50 smallest eigenpairs,
+block size 64, residual ||Ax - lambda Bx|| / (|lambda| ||Bx||) <= 1e-8 for every
+pair (conv_type "BR"). Synthetic, exactly assembled; its spectrum is known in
+closed form and checked on every run.
+
+One step = one complete solve from seeded initial vectors with A and B resident
+in HBM (value) or passed as host CSR arrays (e2e). A and B together are ~0.55 GB,
+larger than the 129 MB L2, so consecutive solves do not run from cache.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 (torchrun): every rank solves its own replica (the solve does not shard);
+the line reports the slowest rank.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gcge-1.0_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "sec to nev eigenpairs @1e-8 residual: mixed-prec vs FP64 GCGE, 1 GB300"
+WORKLOADS = {
+    # name: (ne, nev, block)
+    "fem96": (96, 50, 64),
+    "fem48": (48, 50, 64),
+    "fem24": (24, 20, 24),
+}
+HW_FP64_TFLOPS = 1.199   # measured FP64 FMA throughput of a GB300 (profiles/gb300_throughput_probe.md)
+
+
+def rank_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier and max-reduction across torchrun ranks (gloo, host scalars only)."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = rank_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            self.dist.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_problem(name):
+    from gcge_gb300 import problems as P
+    ne, nev, block = WORKLOADS[name]
+    t0 = time.time()
+    A, B = P.fem_q1_cube(ne)
+    return A, B, nev, block, P.fem_q1_cube_eigs(ne, nev), time.time() - t0
+
+
+def check_solution(A, B, ev, X, exact):
+    """Residuals under the solve's criterion and eigenvalue error against the closed form."""
+    As, Bs = A.to_scipy(), B.to_scipy()
+    AX, BX = As @ X, Bs @ X
+    r = np.linalg.norm(AX - BX * ev[None, :], axis=0) / (np.abs(ev) * np.linalg.norm(BX, axis=0))
+    return float(r.max()), float(np.max(np.abs(ev - exact) / exact))
+
+
+def cpu_sample(workload_full_n, gpu_iters=None, threads=1):
+    """Bounded CPU run: the oracle port (restatement of the reference CSR path, scalar C;
+    OpenBLAS limited to `threads` for the small dense calls) on the same pencil family at
+    ne = 24 (n = 12,167), 50 eigenpairs, block 64, residual <= 1e-8. Its wall time is
+    scaled to the full workload by the row ratio (every per-iteration cost of the path is
+    linear in n at fixed nev) and, when known, by the ratio of GCG iterations."""
+    code = r"""
+import json, os, sys, time
+sys.path.insert(0, %r); sys.path.insert(0, %r)
+import pyoracle
+from gcge_gb300 import problems as P
+A, B = P.fem_q1_cube(24)
+o = pyoracle.Oracle()
+p = o.params(nev=50, block_size=64, ev_max_it=400, conv_type="BR", init_rng=1, seed=7)
+t = time.time(); ev, X, st = o.solve(A, B, p); w = time.time() - t
+print(json.dumps({"wall": w, "iters": st.num_iter, "n": A.n, "unlock": st.num_unlock}))
+""" % (os.path.join(ROOT, "gcge-1.0_gb300"), os.path.join(ROOT, "oracle"))
+    env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
+    if r.returncode != 0:
+        raise RuntimeError("cpu sample failed: " + r.stderr[-2000:])
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    scale_n = workload_full_n / d["n"]
+    scale_it = (gpu_iters / d["iters"]) if gpu_iters else 1.0
+    est = d["wall"] * scale_n * scale_it
+    sample = ("oracle port (C restatement of the reference CSR GCGE), full solve of the Q1 cube at ne=24 "
+              "(n=%d, nev=50, block 64, BR<=1e-8): %.2f s wall, %d GCG iterations; scaled by n ratio %.2f%s"
+              % (d["n"], d["wall"], d["iters"], scale_n,
+                 (" and iteration ratio %d/%d" % (gpu_iters, d["iters"])) if gpu_iters else ""))
+    return est, sample
+
+
+def roofline_from_profile(prof, hbm_peak):
+    total = sum(v["ms"] for v in prof.values()) or 1.0
+    rows = {}
+    for cls, v in prof.items():
+        if v["launches"] == 0:
+            continue
+        t = v["ms"] * 1e-3
+        gbs = v["bytes"] / t / 1e9 if t > 0 else 0.0
+        tfl = v["flops"] / t / 1e12 if t > 0 else 0.0
+        fp64 = cls in ("spmm_fp64", "gram", "lincomb", "dense_gemm")
+        row = {"share": v["ms"] / total, "ms": v["ms"], "launches": v["launches"],
+               "achieved_gbs": gbs, "achieved_tflops": tfl}
+        if fp64:
+            row.update(bound="fp64", peak=HW_FP64_TFLOPS, unit="TFLOP/s", frac=tfl / HW_FP64_TFLOPS,
+                       hbm_frac=gbs / hbm_peak)
+        elif cls == "dense_eig":
+            row.update(bound="latency", peak=None, unit=None, frac=None)
+        else:
+            row.update(bound="hbm", peak=hbm_peak, unit="GB/s", frac=gbs / hbm_peak)
+        rows[cls] = row
+    return rows
+
+
+def load_traffic():
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def run_gb300(args, dist):
+    import gcge_gb300 as G
+    rank = dist.rank
+    A, B, nev, block, exact, gen_s = make_problem(args.workload)
+    hbm_peak, _, peak_kind = peaks()
+    ctx = G.Context(dist.local)
+    dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
+    X = ctx.multivec(A.n, nev)
+
+    def params(prec):
+        return ctx.params(nev=nev, block_size=block, ev_max_it=args.max_it, conv_type="BR", ev_tol=1e-8,
+                          precision=prec, seed=20241203)
+
+    def solve(prec):
+        ev, Xh, st = ctx.solve(dA, dB, params(prec), evec=X)
+        return ev, Xh, st
+
+    for _ in range(args.warmup):
+        solve(1)
+    # ---- timed region: K mixed-precision solves, profiling on (events on the library's stream)
+    sampler = ClockSampler(dist.local)
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    dist.barrier()
+    ctx.sync()
+    sampler.start()
+    t0 = time.time()
+    times, iters, launches = [], [], 0
+    for _ in range(args.steps):
+        ev, Xh, st = solve(1)
+        times.append(st.solve_ms * 1e-3)
+        iters.append(st.num_iter)
+        launches += st.kernel_launches
+        last = (ev, Xh, st)
+    ctx.sync()
+    wall = time.time() - t0
+    dist.barrier()
+    clocks = sampler.stop()
+    prof = ctx.profile_read(reset=True)
+    ctx.profile(False)
+    mixed_s = dist.max(sum(times) / len(times))
+    ev, Xh, st = last
+    res_mixed, err_mixed = check_solution(A, B, ev, Xh, exact)
+    phases = st.as_dict()["phase_ms"]
+    # ---- plain FP64 on the same workload
+    fp64_times, fp64_iters = [], []
+    for i in range(args.fp64_warmup + args.fp64_steps):
+        ev64, X64, st64 = solve(0)
+        if i >= args.fp64_warmup:
+            fp64_times.append(st64.solve_ms * 1e-3)
+            fp64_iters.append(st64.num_iter)
+    fp64_s = dist.max(sum(fp64_times) / len(fp64_times)) if fp64_times else None
+    res64, err64 = check_solution(A, B, ev64, X64, exact)
+    # ---- end to end through the host-buffer C ABI call (uploads + solve + download timed)
+    e2e = []
+    h2d = A.rowptr.nbytes + A.col.nbytes + A.val.nbytes + B.rowptr.nbytes + B.col.nbytes + B.val.nbytes
+    d2h = A.n * nev * 8 + nev * 8
+    for i in range(1 + args.e2e_steps):
+        p = params(1)
+        ctx.sync()
+        t = time.time()
+        ctx.solve_host(A, B, p)
+        if i >= 1:
+            e2e.append(time.time() - t)
+    e2e_s = dist.max(sum(e2e) / len(e2e))
+    out = None
+    if rank == 0:
+        rows = roofline_from_profile(prof, hbm_peak)
+        dom = max(rows, key=lambda c: rows[c]["ms"])
+        d = rows[dom]
+        traffic = load_traffic().get(dom)
+        per_launch_alg = prof[dom]["bytes"] / max(prof[dom]["launches"], 1)
+        spmm32 = rows.get("spmm_fp32")
+        cpu = None
+        if not args.no_cpu_baseline:
+            est, sample = cpu_sample(A.n, gpu_iters=int(round(statistics.mean(iters))), threads=1)
+            cpu = {"value": est, "unit": "s", "cores": 1, "kind": "port", "sample": sample}
+        out = {
+            "metric": METRIC, "value": mixed_s, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mixed_s * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64 + fp32 inner block CG",
+            "data": "synthetic (exactly assembled Q1 FEM pencil, closed-form spectrum)",
+            "config": {"workload": "Q1 FEM cube %d^3 elements, n=%d, nnz(A)=%d, nnz(B)=%d, nev=%d, block=%d, "
+                                   "residual ||Ax-lBx||/(|l||Bx||)<=1e-8" % (WORKLOADS[args.workload][0], A.n,
+                                                                              A.nnz, B.nnz, nev, block),
+                       "form": "mixed", "parallelism": "replicas" if dist.world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (A+B %.0f MB > 129 MB)" % (h2d / 1e6),
+                       "problem_generation_s": gen_s},
+            "fp64": {"value": fp64_s, "unit": "s", "iterations": fp64_iters, "max_residual": res64,
+                     "max_rel_eig_err": err64},
+            "speedup_mixed_vs_fp64": (fp64_s / mixed_s) if fp64_s else None,
+            "mixed": {"iterations": iters, "max_residual": res_mixed, "max_rel_eig_err": err_mixed,
+                      "wall_s_timed_region": wall, "phase_ms_last_step": phases},
+            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": {"kernel": dom, "bound": d["bound"], "achieved": d["achieved_tflops"] if d["bound"] == "fp64"
+                         else d["achieved_gbs"], "peak": d["peak"], "unit": d["unit"], "frac": d["frac"],
+                         "peak_source": ("FP64 FMA throughput measured on GB300 (profiles)" if d["bound"] == "fp64"
+                                         else "MEASURED_PEAKS.json hbm_gbs (%s)" % peak_kind),
+                         "traffic": traffic, "alg_bytes_per_launch": per_launch_alg,
+                         "share_of_kernel_time": d["share"]},
+            "roofline_spmm_fp32": ({"bound": "hbm", "achieved": spmm32["achieved_gbs"], "peak": hbm_peak,
+                                    "unit": "GB/s", "frac": spmm32["frac"],
+                                    "traffic": load_traffic().get("spmm_fp32")} if spmm32 else None),
+            "kernels": rows,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+    ctx.close()
+    return out
+
+
+def run_reference(args, dist):
+    """The reference arm: the oracle port of the reference CSR GCGE (the compiled reference
+    is x86-only in this tree) on the host cores, same workload, metric and unit."""
+    if dist.rank != 0:
+        return None
+    from gcge_gb300 import problems as P
+    ne, nev, block = WORKLOADS[args.workload]
+    n_full = (ne - 1) ** 3
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        est, sample = cpu_sample(n_full, gpu_iters=None, threads=threads)
+        if i >= args.warmup:
+            vals.append(est)
+    v = statistics.mean(vals)
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "config": {"workload": "Q1 FEM cube %d^3 elements, n=%d, nev=%d, block=%d, BR<=1e-8"
+                                   % (ne, n_full, nev, block), "form": "reference CPU path"},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="fem96", choices=sorted(WORKLOADS))
+    ap.add_argument("--max-it", type=int, default=400)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--fp64-warmup", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
+    if out is not None and dist.rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,325 @@
+// gb_bcg.cu -- block conjugate gradients on GB300, GCGE_BCG semantics
+// (src/gcge_cg.c:137-302) with all control state on the device.
+//
+// Per-column scalars rho1, rho2, ptw, err and the active-column count live in
+// device memory; every kernel reads the count and leaves columns at or beyond it
+// untouched, so the loop runs cg_max_it-1 rounds without a host round trip and
+// a round with no active column costs only its launches.
+//
+// The active set follows the reference exactly: after each round the count of
+// columns whose residual ratio ||r_k||/||r_0|| is still >= cg_rate is taken
+// over all columns, and the next round updates the first `count` columns
+// (src/gcge_cg.c:713-720 writes unlock[idx] = idx at position idx, and the
+// update loops walk unlock[0 .. num_unlock)).
+//
+// precision 0: FP64 vectors and values. precision 1: the residual of the initial
+// guess is formed in FP64, then CG runs on the correction with FP32 vectors and
+// the FP32 copy of the matrix values; products are formed in FP32 and summed in
+// FP32 over runs of 8 rows, then accumulated in FP64 (FP64-reduced dot products);
+// the correction is added to the FP64 solution at the end.
+#include <cuda_runtime.h>
+
+#include "gb_internal.h"
+
+#define RED_ROWS 1024
+
+extern "C" int gb_axpy32(gcge_gpu_ctx *ctx, int n, int k, float a, const float *X, float *Y, long ld);
+
+static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+#define GB_PROF(ctx, cls, bytes, flops) \
+    do { if ((ctx)->prof) gb_prof_begin((ctx), (cls), (bytes), (flops)); } while (0)
+
+#define GB_LAUNCH(ctx, kern, grid, block, smem, ...)                                   \
+    do {                                                                               \
+        kern<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);                 \
+        (ctx)->launches++;                                                             \
+        if ((ctx)->prof) gb_prof_end(ctx);                                             \
+        int _st = gb_check_launch(ctx);                                                \
+        if (_st) return _st;                                                           \
+    } while (0)
+
+struct bcg_state {
+    double *rho1, *rho2, *err, *ptw, *part;
+    int *nact;
+};
+
+// p = r + beta p on active columns (beta = 0 on the first round: p = r)
+template <typename T>
+__global__ void k_pupdate(int n, int k, const T *__restrict__ R, T *__restrict__ P, long ld,
+                          const double *__restrict__ rho1, const double *__restrict__ rho2,
+                          const int *__restrict__ nact, int first)
+{
+    const int ka = *nact;
+    if (ka <= 0) return;
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        if (c >= ka) continue;
+        if (first) {
+            P[r * ld + c] = R[r * ld + c];
+        } else {
+            const T beta = (T)(rho2[c] / rho1[c]);
+            P[r * ld + c] = R[r * ld + c] + beta * P[r * ld + c];
+        }
+    }
+}
+
+// partial sums of a*b over row slabs, active columns only
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_dot_partial(int n, int k, const T *__restrict__ A, const T *__restrict__ B, long ld,
+              const int *__restrict__ nact, double *__restrict__ part)
+{
+    __shared__ double sh[8][33];
+    const int ka = nact ? *nact : k;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int c = blockIdx.y * 32 + tx;
+    const long r0 = (long)blockIdx.x * RED_ROWS, r1 = min((long)n, r0 + RED_ROWS);
+    double s = 0;
+    if (c < k && c < ka) {
+        long r = r0 + ty;
+        while (r < r1) {
+            T run = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q, r += 8)
+                if (r < r1) run = fma(A[r * ld + c], B[r * ld + c], run);
+            s += (double)run;
+        }
+    }
+    sh[ty][tx] = s;
+    __syncthreads();
+    if (ty == 0 && c < k) {
+        double t = 0;
+        for (int q = 0; q < 8; ++q) t += sh[q][tx];
+        part[(long)blockIdx.x * k + c] = t;
+    }
+}
+
+// x += alpha p, r -= alpha w (alpha = rho2/ptw) on active columns, with the
+// partial sums of the new r.r
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_xr_update(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restrict__ P,
+            const T *__restrict__ W, long ld, const double *__restrict__ rho2, const double *__restrict__ ptw,
+            const int *__restrict__ nact, double *__restrict__ part)
+{
+    __shared__ double sh[8][33];
+    const int ka = *nact;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int c = blockIdx.y * 32 + tx;
+    const long r0 = (long)blockIdx.x * RED_ROWS, r1 = min((long)n, r0 + RED_ROWS);
+    double s = 0;
+    if (c < k && c < ka) {
+        const double ad = rho2[c] / ptw[c];
+        const T a = (T)ad;
+        long r = r0 + ty;
+        while (r < r1) {
+            T run = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q, r += 8) {
+                if (r < r1) {
+                    const long o = r * ld + c;
+                    X[o] = X[o] + a * P[o];
+                    const T rn = R[o] - a * W[o];
+                    R[o] = rn;
+                    run = fma(rn, rn, run);
+                }
+            }
+            s += (double)run;
+        }
+    }
+    sh[ty][tx] = s;
+    __syncthreads();
+    if (ty == 0 && c < k && c < ka) {
+        double t = 0;
+        for (int q = 0; q < 8; ++q) t += sh[q][tx];
+        part[(long)blockIdx.x * k + c] = t;
+    }
+}
+
+// ptw[c] = sum of partials for active c
+__global__ void k_sum_active(int nblk, int k, const double *__restrict__ part, const int *__restrict__ nact,
+                             double *__restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k || c >= *nact) return;
+    double s = 0;
+    for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
+    out[c] = s;
+}
+
+// initial residual norms: rho2 = sum partials, err = sqrt(rho2), nact = k
+__global__ void k_init_state(int nblk, int k, const double *__restrict__ part, double *rho2, double *err,
+                             int *nact)
+{
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        double s = 0;
+        for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
+        rho2[c] = s;
+        err[c] = sqrt(s);
+    }
+    if (threadIdx.x == 0) *nact = k;
+}
+
+// end of a round: rho1 = rho2, rho2 = new r.r (active columns); recount over all columns
+__global__ void k_finalize(int nblk, int k, const double *__restrict__ part, double *rho1, double *rho2,
+                           const double *__restrict__ err, int *nact, double rate)
+{
+    __shared__ int cnt;
+    const int ka = *nact;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        if (c < ka) {
+            double s = 0;
+            for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
+            rho1[c] = rho2[c];
+            rho2[c] = s;
+        }
+        const double lerr = sqrt(fabs(rho2[c]));
+        if (lerr / err[c] >= rate) atomicAdd(&cnt, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *nact = cnt;
+}
+
+// X += (double) D
+__global__ void k_add_f2d(int n, int k, const float *__restrict__ D, long ldd, double *__restrict__ X, long ldx)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        X[r * ldx + c] += (double)D[r * ldd + c];
+    }
+}
+
+static int elem_grid(gcge_gpu_ctx *ctx, long total)
+{
+    long g = (total + 255) / 256, cap = (long)ctx->num_sms * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
+{
+    long ldk = (k + 1) & ~1;
+    size_t vec = precision ? sizeof(float) : sizeof(double);
+    size_t nblk = (size_t)cdiv(n > 0 ? n : 1, RED_ROWS);
+    size_t blocks = 4 * (size_t)n * ldk * vec;  // R, X, P, W
+    size_t state = (4 * (size_t)k + nblk * (size_t)k + 8) * sizeof(double) + 64;
+    return blocks + state + 16 * 256;   // every sub-buffer is aligned to 256 bytes (10 of them)
+}
+
+template <typename T>
+static int bcg_rounds(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, T *R, T *X, T *P, T *W, long ld,
+                      const gb_bcg_args *a, bcg_state *s)
+{
+    const int n = a->n, k = a->k, nblk = cdiv(n > 0 ? n : 1, RED_ROWS);
+    dim3 rgrid(nblk, (k + 31) / 32);
+    const double es = sizeof(T);
+    for (int it = 1; it < a->max_it; ++it) {
+        GB_PROF(ctx, GB_K_BCGVEC, 3.0 * es * n * k, 2.0 * n * k);
+        GB_LAUNCH(ctx, k_pupdate<T>, elem_grid(ctx, (long)n * k), 256, 0, n, k, R, P, ld, s->rho1, s->rho2,
+                  s->nact, it == 1);
+        int st;
+        if (sizeof(T) == sizeof(double))
+            st = gb_spmm(ctx, A, (const double *)P, ld, (double *)W, ld, k, 1.0, nullptr, 0.0, s->nact);
+        else
+            st = gb_spmm32(ctx, A, (const float *)P, ld, (float *)W, ld, k, s->nact);
+        if (st) return st;
+        GB_PROF(ctx, GB_K_BCGVEC, 2.0 * es * n * k, 2.0 * n * k);
+        GB_LAUNCH(ctx, k_dot_partial<T>, rgrid, 256, 0, n, k, P, W, ld, s->nact, s->part);
+        GB_LAUNCH(ctx, k_sum_active, (k + 127) / 128, 128, 0, nblk, k, s->part, s->nact, s->ptw);
+        GB_PROF(ctx, GB_K_BCGVEC, 6.0 * es * n * k, 6.0 * n * k);
+        GB_LAUNCH(ctx, k_xr_update<T>, rgrid, 256, 0, n, k, X, R, P, W, ld, s->rho2, s->ptw, s->nact, s->part);
+        GB_LAUNCH(ctx, k_finalize, 1, 256, 0, nblk, k, s->part, s->rho1, s->rho2, s->err, s->nact, a->rate);
+    }
+    return GCGE_GPU_OK;
+}
+
+extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, long ldr, double *X, long ldx,
+                      const gb_bcg_args *a, void *work, size_t work_bytes)
+{
+    const int n = a->n, k = a->k;
+    if (k <= 0 || n <= 0) return GCGE_GPU_OK;
+    if (work_bytes < gb_bcg_work_bytes(n, k, a->precision)) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    if (a->precision && !A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    const long ld = (k + 1) & ~1;
+    const int nblk = cdiv(n, RED_ROWS);
+    char *w = (char *)work;
+    size_t vec = a->precision ? sizeof(float) : sizeof(double);
+    auto take = [&](size_t bytes) { char *p = w; w += (bytes + 255) & ~(size_t)255; return (void *)p; };
+    bcg_state s;
+    s.rho1 = (double *)take(sizeof(double) * k);
+    s.rho2 = (double *)take(sizeof(double) * k);
+    s.err = (double *)take(sizeof(double) * k);
+    s.ptw = (double *)take(sizeof(double) * k);
+    s.part = (double *)take(sizeof(double) * (size_t)nblk * k);
+    s.nact = (int *)take(64);
+    dim3 rgrid(nblk, (k + 31) / 32);
+    if (a->precision == 0) {
+        double *P = (double *)take((size_t)n * ld * vec);
+        double *W = (double *)take((size_t)n * ld * vec);
+        (void)W;
+        // R = RHS - A X, in place in RHS (the reference overwrites RHS with the residual)
+        int st = gb_spmm(ctx, A, X, ldx, RHS, ldr, k, -1.0, nullptr, 1.0, nullptr);
+        if (st) return st;
+        // P and W use the compact ld; R and X keep their own ld through the copies below
+        if (ldr == ld && ldx == ld) {
+            GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, RHS, RHS, ld, (const int *)nullptr, s.part);
+            GB_LAUNCH(ctx, k_init_state, 1, 256, 0, nblk, k, s.part, s.rho2, s.err, s.nact);
+            return bcg_rounds<double>(ctx, A, RHS, X, P, W, ld, a, &s);
+        }
+        // general leading dimensions: stage R and X in compact blocks
+        double *R = (double *)take((size_t)n * ld * vec);
+        double *Xc = (double *)take((size_t)n * ld * vec);
+        if ((size_t)(w - (char *)work) > work_bytes) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+        if ((st = gb_axpby(ctx, n, k, 1.0, RHS, ldr, 0.0, R, ld))) return st;
+        if ((st = gb_axpby(ctx, n, k, 1.0, X, ldx, 0.0, Xc, ld))) return st;
+        GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
+        GB_LAUNCH(ctx, k_init_state, 1, 256, 0, nblk, k, s.part, s.rho2, s.err, s.nact);
+        if ((st = bcg_rounds<double>(ctx, A, R, Xc, P, W, ld, a, &s))) return st;
+        if ((st = gb_axpby(ctx, n, k, 1.0, Xc, ld, 0.0, X, ldx))) return st;
+        return gb_axpby(ctx, n, k, 1.0, R, ld, 0.0, RHS, ldr);
+    }
+    // Mixed precision as defect correction: the residual r0 = RHS - A X is formed in
+    // FP64, block CG runs in FP32 on A D = r0 from D = 0, and X += D in FP64. The
+    // iteration is the reference's in exact arithmetic, while the correction D, not
+    // the whole solution, carries the FP32 rounding.
+    float *R = (float *)take((size_t)n * ld * vec);
+    float *D = (float *)take((size_t)n * ld * vec);
+    float *P = (float *)take((size_t)n * ld * vec);
+    float *W = (float *)take((size_t)n * ld * vec);
+    if ((size_t)(w - (char *)work) > work_bytes) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    int st;
+    if ((st = gb_spmm(ctx, A, X, ldx, RHS, ldr, k, -1.0, nullptr, 1.0, nullptr))) return st;
+    if ((st = gb_convert_d2f(ctx, n, k, RHS, ldr, R, ld))) return st;
+    if (cudaMemsetAsync(D, 0, (size_t)n * ld * sizeof(float), ctx->stream) != cudaSuccess)
+        return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+    GB_LAUNCH(ctx, k_dot_partial<float>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
+    GB_LAUNCH(ctx, k_init_state, 1, 256, 0, nblk, k, s.part, s.rho2, s.err, s.nact);
+    if ((st = bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s))) return st;
+    GB_LAUNCH(ctx, k_add_f2d, elem_grid(ctx, (long)n * k), 256, 0, n, k, D, ld, X, ldx);
+    return gb_convert_f2d(ctx, n, k, R, ld, RHS, ldr);
+}
+
+__global__ void k_axpy32(int n, int k, float a, const float *__restrict__ X, float *__restrict__ Y, long ld)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        Y[r * ld + c] += a * X[r * ld + c];
+    }
+}
+
+extern "C" int gb_axpy32(gcge_gpu_ctx *ctx, int n, int k, float a, const float *X, float *Y, long ld)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_axpy32, elem_grid(ctx, (long)n * k), 256, 0, n, k, a, X, Y, ld);
+    return GCGE_GPU_OK;
+}

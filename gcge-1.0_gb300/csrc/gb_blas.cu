@@ -1,0 +1,567 @@
+// gb_blas.cu -- HBM-streaming kernels of the GCGE hot path on GB300 (sm_103a).
+//
+//  * CSR SpMM against row-major multivector blocks (FP64 and FP32 values):
+//    one warp per (row, 64-column chunk); the row's (column, value) pairs are
+//    loaded once per 32 entries with coalesced loads and broadcast by shuffles,
+//    and every nonzero gathers one contiguous block row of X.
+//  * AXPBY / gathers / conversions: grid-stride element kernels.
+//  * Per-column dot products, residual norms and tall-skinny Gram products:
+//    deterministic two-stage reductions (fixed partition of the rows, partials
+//    in scratch, fixed-order second stage), so results do not depend on timing.
+//  * Linear combinations X*C: 64-row x 32-column output tiles with X and C
+//    staged in shared memory.
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "gb_internal.h"
+
+#define FULL 0xffffffffu
+
+static inline int ceil_div_l(long a, long b) { return (int)((a + b - 1) / b); }
+
+#define GB_LAUNCH(ctx, kern, grid, block, smem, ...)                                   \
+    do {                                                                               \
+        kern<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);                 \
+        (ctx)->launches++;                                                             \
+        if ((ctx)->prof) gb_prof_end(ctx);                                             \
+        int _st = gb_check_launch(ctx);                                                \
+        if (_st) return _st;                                                           \
+    } while (0)
+
+// profile the next launch (no-op unless profiling is enabled on the context)
+#define GB_PROF(ctx, cls, bytes, flops) \
+    do { if ((ctx)->prof) gb_prof_begin((ctx), (cls), (bytes), (flops)); } while (0)
+
+// ---------------------------------------------------------------- SpMM
+// Y[row, c] = alpha * alpha_col[c] * sum_j A[row, j] X[j, c] + beta * Y[row, c]
+template <typename VT, typename XT, typename AT>
+__global__ void __launch_bounds__(256)
+k_spmm(int n, const int *__restrict__ rp, const int *__restrict__ ci, const VT *__restrict__ val,
+       const XT *__restrict__ X, long ldx, XT *__restrict__ Y, long ldy, int k, AT alpha,
+       const double *__restrict__ alpha_col, AT beta, const int *__restrict__ ncols_dev)
+{
+    const int lane = threadIdx.x & 31;
+    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nchunks = (k + 63) >> 6;
+    if (warp >= (long)n * nchunks) return;                 // warp-uniform
+    int kact = k;
+    if (ncols_dev) kact = min(k, *ncols_dev);
+    const int row = (int)(warp / nchunks);
+    const int chunk = (int)(warp - (long)row * nchunks);
+    const int c0 = chunk * 64 + lane, c1 = c0 + 32;
+    if (chunk * 64 >= kact) return;                        // warp-uniform
+    const bool h0 = c0 < kact, h1 = c1 < kact;
+    AT acc0 = 0, acc1 = 0;
+    const int beg = rp[row], end = rp[row + 1];
+    for (int base = beg; base < end; base += 32) {
+        const int e = base + lane;
+        int j = 0;
+        VT a = 0;
+        if (e < end) { j = __ldg(ci + e); a = __ldg(val + e); }
+        const int cnt = min(32, end - base);
+        for (int t = 0; t < cnt; ++t) {
+            const int jj = __shfl_sync(FULL, j, t);
+            const AT aa = (AT)__shfl_sync(FULL, a, t);
+            const XT *xr = X + (long)jj * ldx;
+            if (h0) acc0 = fma(aa, (AT)__ldg(xr + c0), acc0);
+            if (h1) acc1 = fma(aa, (AT)__ldg(xr + c1), acc1);
+        }
+    }
+    XT *yr = Y + (long)row * ldy;
+    if (h0) {
+        AT s = alpha * (alpha_col ? (AT)alpha_col[c0] : (AT)1);
+        yr[c0] = (XT)(beta == (AT)0 ? s * acc0 : s * acc0 + beta * (AT)yr[c0]);
+    }
+    if (h1) {
+        AT s = alpha * (alpha_col ? (AT)alpha_col[c1] : (AT)1);
+        yr[c1] = (XT)(beta == (AT)0 ? s * acc1 : s * acc1 + beta * (AT)yr[c1]);
+    }
+}
+
+// single-column SpMV: a warp splits the row's nonzeros, shuffle reduction
+template <typename VT, typename XT, typename AT>
+__global__ void __launch_bounds__(256)
+k_spmv(int n, const int *__restrict__ rp, const int *__restrict__ ci, const VT *__restrict__ val,
+       const XT *__restrict__ X, long ldx, XT *__restrict__ Y, long ldy, AT alpha,
+       const double *__restrict__ alpha_col, AT beta, const int *__restrict__ ncols_dev)
+{
+    const int lane = threadIdx.x & 31;
+    const long row = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    if (ncols_dev && *ncols_dev < 1) return;
+    AT acc = 0;
+    for (int e = rp[row] + lane; e < rp[row + 1]; e += 32)
+        acc = fma((AT)__ldg(val + e), (AT)__ldg(X + (long)__ldg(ci + e) * ldx), acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+    if (lane == 0) {
+        AT s = alpha * (alpha_col ? (AT)alpha_col[0] : (AT)1);
+        Y[row * ldy] = (XT)(beta == (AT)0 ? s * acc : s * acc + beta * (AT)Y[row * ldy]);
+    }
+}
+
+extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X, long ldx, double *Y,
+                       long ldy, int k, double alpha, const double *alpha_col, double beta,
+                       const int *ncols_dev)
+{
+    if (k <= 0 || A->n <= 0) return GCGE_GPU_OK;
+    ctx->spmm_launches++;
+    GB_PROF(ctx, GB_K_SPMM64, 12.0 * A->nnz + 4.0 * (A->n + 1) + (beta != 0.0 ? 24.0 : 16.0) * A->n * k,
+            2.0 * A->nnz * k);
+    if (k == 1) {
+        int grid = ceil_div_l((long)A->n * 32, 256);
+        GB_LAUNCH(ctx, (k_spmv<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
+                  Y, ldy, alpha, alpha_col, beta, ncols_dev);
+    } else {
+        long warps = (long)A->n * ((k + 63) / 64);
+        int grid = ceil_div_l(warps * 32, 256);
+        GB_LAUNCH(ctx, (k_spmm<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
+                  Y, ldy, k, alpha, alpha_col, beta, ncols_dev);
+    }
+    return GCGE_GPU_OK;
+}
+
+extern "C" int gb_spmm32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const float *X, long ldx, float *Y,
+                         long ldy, int k, const int *ncols_dev)
+{
+    if (k <= 0 || A->n <= 0) return GCGE_GPU_OK;
+    if (!A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    ctx->spmm_launches++;
+    GB_PROF(ctx, GB_K_SPMM32, 8.0 * A->nnz + 4.0 * (A->n + 1) + 8.0 * A->n * k, 2.0 * A->nnz * k);
+    if (k == 1) {
+        int grid = ceil_div_l((long)A->n * 32, 256);
+        GB_LAUNCH(ctx, (k_spmv<float, float, float>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx,
+                  Y, ldy, 1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+    } else {
+        long warps = (long)A->n * ((k + 63) / 64);
+        int grid = ceil_div_l(warps * 32, 256);
+        GB_LAUNCH(ctx, (k_spmm<float, float, float>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y,
+                  ldy, k, 1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+    }
+    return GCGE_GPU_OK;
+}
+
+// ---------------------------------------------------------------- AXPBY
+__global__ void k_axpby(int n, int k, double a, const double *__restrict__ X, long ldx, double b,
+                        double *__restrict__ Y, long ldy)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        double *y = Y + r * ldy + c;
+        if (a == 0.0) *y = b * *y;
+        else if (b == 0.0) *y = (a == 1.0) ? X[r * ldx + c] : a * X[r * ldx + c];
+        else *y = a * X[r * ldx + c] + b * *y;
+    }
+}
+
+static int elem_grid(gcge_gpu_ctx *ctx, long total)
+{
+    long g = (total + 255) / 256;
+    long cap = (long)ctx->num_sms * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+extern "C" int gb_axpby(gcge_gpu_ctx *ctx, int n, int k, double a, const double *X, long ldx, double b,
+                        double *Y, long ldy)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    GB_PROF(ctx, GB_K_BLAS1, (a == 0.0 || b == 0.0 ? 16.0 : 24.0) * n * k, 2.0 * n * k);
+    GB_LAUNCH(ctx, k_axpby, elem_grid(ctx, (long)n * k), 256, 0, n, k, a, X, ldx, b, Y, ldy);
+    return GCGE_GPU_OK;
+}
+
+__global__ void k_gather_cols(int n, int k, const double *__restrict__ X, long ldx, const int *__restrict__ idx,
+                              double *__restrict__ Y, long ldy, const double *__restrict__ eval, int mode)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        const int src = idx ? idx[c] : c;
+        double s = 1.0;
+        if (mode == 1) {
+            const double l = eval[src];
+            s = fabs(l) <= 1.0 ? 1.0 : 1.0 / l;
+        }
+        const double x = X[r * ldx + src];
+        Y[r * ldy + c] = (mode == 1 && s != 1.0) ? s * x : x;
+    }
+}
+
+extern "C" int gb_gather_cols(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, const int *idx_dev,
+                              double *Y, long ldy, const double *eval_dev, int mode)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_gather_cols, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, idx_dev, Y, ldy,
+              eval_dev, mode);
+    return GCGE_GPU_OK;
+}
+
+__global__ void k_fill_random(int n, int k, double *X, long ldx, int col0, unsigned long long seed)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        unsigned long long z = seed ^ ((unsigned long long)((long)(col0 + c) * n + r) * 0xD1B54A32D192ED03ULL);
+        z += 0x9E3779B97F4A7C15ULL;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        X[r * ldx + c] = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    }
+}
+
+extern "C" int gb_fill_random(gcge_gpu_ctx *ctx, int n, int k, double *X, long ldx, int col0,
+                              unsigned long long seed)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_fill_random, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, col0, seed);
+    return GCGE_GPU_OK;
+}
+
+__global__ void k_d2f(int n, int k, const double *__restrict__ X, long ldx, float *__restrict__ Y, long ldy)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        Y[r * ldy + c] = (float)X[r * ldx + c];
+    }
+}
+__global__ void k_f2d(int n, int k, const float *__restrict__ X, long ldx, double *__restrict__ Y, long ldy)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        Y[r * ldy + c] = (double)X[r * ldx + c];
+    }
+}
+extern "C" int gb_convert_d2f(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, float *Y, long ldy)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_d2f, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, Y, ldy);
+    return GCGE_GPU_OK;
+}
+extern "C" int gb_convert_f2d(gcge_gpu_ctx *ctx, int n, int k, const float *X, long ldx, double *Y, long ldy)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_f2d, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, Y, ldy);
+    return GCGE_GPU_OK;
+}
+
+// Dirichlet rows (app/csr/gcge_app_csr.c:130-183): B row has no |b| > 1e-20 and
+// the A row exactly one |a| > 1e-20 -> zero that row of X.
+__global__ void k_dirichlet(int n, const int *arp, const double *av, const int *brp, const double *bv, int k,
+                            double *X, long ldx)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        bool zero_b = true;
+        for (int j = brp[i]; j < brp[i + 1]; ++j)
+            if (fabs(bv[j]) > 1e-20) { zero_b = false; break; }
+        if (!zero_b) continue;
+        int cnt = 0;
+        for (int j = arp[i]; j < arp[i + 1]; ++j)
+            if (fabs(av[j]) > 1e-20) cnt++;
+        if (cnt == 1)
+            for (int c = 0; c < k; ++c) X[(long)i * ldx + c] = 0.0;
+    }
+}
+extern "C" int gb_dirichlet_zero(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B, int k,
+                                 double *X, long ldx)
+{
+    if (!A || !B || k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_dirichlet, elem_grid(ctx, A->n), 256, 0, A->n, A->rp, A->v, B->rp, B->v, k, X, ldx);
+    return GCGE_GPU_OK;
+}
+
+// ---------------------------------------------------------------- per-column reductions
+// Stage 1: block b covers rows [b*R, (b+1)*R) (R fixed by n), 32-column slab per
+// blockIdx.y; partial[b * k + c]. Stage 2: fixed-order sum over b.
+#define RED_ROWS 1024
+template <int MODE>
+__global__ void __launch_bounds__(256)
+k_coldot_partial(int n, int k, const double *__restrict__ X, long ldx, const double *__restrict__ Y, long ldy,
+                 const double *__restrict__ Z, long ldz, const double *__restrict__ eval,
+                 const int *__restrict__ idx, double *__restrict__ part)
+{
+    // MODE 0: sum X*Y. MODE 1: residual triple (sum (Y - l Z)^2, sum X^2, sum Z^2), Z may be NULL (= X).
+    __shared__ double sh[3][8][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int c = blockIdx.y * 32 + tx;
+    const long r0 = (long)blockIdx.x * RED_ROWS;
+    const long r1 = min((long)n, r0 + RED_ROWS);
+    double s0 = 0, s1 = 0, s2 = 0;
+    if (c < k) {
+        double l = 0;
+        if (MODE == 1) l = eval[idx ? idx[c] : c];
+        for (long r = r0 + ty; r < r1; r += 8) {
+            if (MODE == 0) {
+                s0 = fma(X[r * ldx + c], Y[r * ldy + c], s0);
+            } else {
+                const double x = X[r * ldx + c];
+                const double bx = Z ? Z[r * ldz + c] : x;
+                const double res = Y[r * ldy + c] - l * bx;
+                s0 = fma(res, res, s0);
+                s1 = fma(x, x, s1);
+                s2 = fma(bx, bx, s2);
+            }
+        }
+    }
+    sh[0][ty][tx] = s0;
+    sh[1][ty][tx] = s1;
+    sh[2][ty][tx] = s2;
+    __syncthreads();
+    if (ty == 0 && c < k) {
+        double t0 = 0, t1 = 0, t2 = 0;
+        for (int q = 0; q < 8; ++q) { t0 += sh[0][q][tx]; t1 += sh[1][q][tx]; t2 += sh[2][q][tx]; }
+        const int w = MODE == 0 ? 1 : 3;
+        double *p = part + ((long)blockIdx.x * k + c) * w;
+        p[0] = t0;
+        if (MODE == 1) { p[1] = t1; p[2] = t2; }
+    }
+}
+
+__global__ void k_sum_partials(int nblk, int width, const double *__restrict__ part, double *__restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= width) return;
+    double s = 0;
+    for (int b = 0; b < nblk; ++b) s += part[(long)b * width + c];
+    out[c] = s;
+}
+
+extern "C" int gb_col_dots(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, const double *Y,
+                           long ldy, double *out_dev)
+{
+    if (k <= 0) return GCGE_GPU_OK;
+    const int nblk = ceil_div_l(n > 0 ? n : 1, RED_ROWS);
+    int st = gb_scratch(ctx, (size_t)nblk * k);
+    if (st) return st;
+    dim3 grid(nblk, (k + 31) / 32);
+    GB_PROF(ctx, GB_K_REDUCE, 16.0 * n * k, 2.0 * n * k);
+    GB_LAUNCH(ctx, k_coldot_partial<0>, grid, 256, 0, n, k, X, ldx, Y, ldy, (const double *)nullptr, 0L,
+              (const double *)nullptr, (const int *)nullptr, ctx->scratch);
+    GB_LAUNCH(ctx, k_sum_partials, (k + 127) / 128, 128, 0, nblk, k, ctx->scratch, out_dev);
+    return GCGE_GPU_OK;
+}
+
+extern "C" int gb_residual_norms(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, const double *AX,
+                                 long ldax, const double *BX, long ldbx, const double *eval_dev,
+                                 const int *idx_dev, double *out_dev)
+{
+    if (k <= 0) return GCGE_GPU_OK;
+    const int nblk = ceil_div_l(n > 0 ? n : 1, RED_ROWS);
+    int st = gb_scratch(ctx, (size_t)nblk * k * 3);
+    if (st) return st;
+    dim3 grid(nblk, (k + 31) / 32);
+    GB_PROF(ctx, GB_K_REDUCE, (BX ? 24.0 : 16.0) * n * k, 8.0 * n * k);
+    GB_LAUNCH(ctx, k_coldot_partial<1>, grid, 256, 0, n, k, X, ldx, AX, ldax, BX, ldbx, eval_dev, idx_dev,
+              ctx->scratch);
+    GB_LAUNCH(ctx, k_sum_partials, (3 * k + 127) / 128, 128, 0, nblk, 3 * k, ctx->scratch, out_dev);
+    return GCGE_GPU_OK;
+}
+
+// ---------------------------------------------------------------- Gram V^T W
+// grid (tiles_i, tiles_j, splits); 32x32 output tile, each thread 2x2 outputs;
+// 32-row slabs of V and W staged in shared memory.
+__global__ void __launch_bounds__(256)
+k_gram_partial(int n, int k1, int k2, const double *__restrict__ V, long ldv, const double *__restrict__ W,
+               long ldw, double *__restrict__ part, long rows_per_split, int sym)
+{
+    const int ti = blockIdx.x, tj = blockIdx.y, split = blockIdx.z;
+    if (sym && ti > tj) return;
+    const int i0 = ti * 32, j0 = tj * 32;
+    const long rb = (long)split * rows_per_split;
+    const long re = min((long)n, rb + rows_per_split);
+    __shared__ double Vs[32][33];
+    __shared__ double Ws[32][33];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double a00 = 0, a01 = 0, a10 = 0, a11 = 0;
+    for (long r0 = rb; r0 < re; r0 += 32) {
+        for (int e = threadIdx.x; e < 1024; e += 256) {
+            const int rr = e >> 5, cc = e & 31;
+            const long r = r0 + rr;
+            Vs[rr][cc] = (r < re && i0 + cc < k1) ? V[r * ldv + i0 + cc] : 0.0;
+            Ws[rr][cc] = (r < re && j0 + cc < k2) ? W[r * ldw + j0 + cc] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int rr = 0; rr < 32; ++rr) {
+            const double v0 = Vs[rr][2 * ty], v1 = Vs[rr][2 * ty + 1];
+            const double w0 = Ws[rr][2 * tx], w1 = Ws[rr][2 * tx + 1];
+            a00 = fma(v0, w0, a00);
+            a01 = fma(v0, w1, a01);
+            a10 = fma(v1, w0, a10);
+            a11 = fma(v1, w1, a11);
+        }
+        __syncthreads();
+    }
+    double *p = part + (long)split * k1 * k2;
+    const int i = i0 + 2 * ty, j = j0 + 2 * tx;
+    if (i < k1 && j < k2) p[i + (long)j * k1] = a00;
+    if (i < k1 && j + 1 < k2) p[i + (long)(j + 1) * k1] = a01;
+    if (i + 1 < k1 && j < k2) p[i + 1 + (long)j * k1] = a10;
+    if (i + 1 < k1 && j + 1 < k2) p[i + 1 + (long)(j + 1) * k1] = a11;
+}
+
+__global__ void k_gram_reduce(int k1, int k2, int nsplit, const double *__restrict__ part, double *a, int lda,
+                              int sym)
+{
+    const long total = (long)k1 * k2;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % k1), j = (int)(t / k1);
+        if (sym && i > j) continue;
+        double s = 0;
+        for (int q = 0; q < nsplit; ++q) s += part[(long)q * total + t];
+        a[i + (long)j * lda] = s;
+        if (sym && i != j) a[j + (long)i * lda] = s;
+    }
+}
+
+extern "C" int gb_gram(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *V, long ldv, const double *W,
+                       long ldw, double *a_dev, int lda, int sym)
+{
+    if (k1 <= 0 || k2 <= 0) return GCGE_GPU_OK;
+    const int ti = (k1 + 31) / 32, tj = (k2 + 31) / 32;
+    int tiles = sym ? ti * (ti + 1) / 2 : ti * tj;
+    if (tiles < 1) tiles = 1;
+    long target = (long)ctx->num_sms * 4;
+    long nsplit = target / tiles;
+    long max_split = (n + 255) / 256;
+    if (nsplit > max_split) nsplit = max_split;
+    if (nsplit < 1) nsplit = 1;
+    long rps = ((n + nsplit - 1) / nsplit + 31) / 32 * 32;
+    if (rps < 32) rps = 32;
+    nsplit = (n + rps - 1) / rps;
+    if (nsplit < 1) nsplit = 1;
+    int st = gb_scratch(ctx, (size_t)nsplit * k1 * k2);
+    if (st) return st;
+    dim3 grid(ti, tj, (unsigned)nsplit);
+    GB_PROF(ctx, GB_K_GRAM, 8.0 * n * (k1 + k2), sym ? 1.0 * n * k1 * (k1 + 1) : 2.0 * n * k1 * k2);
+    GB_LAUNCH(ctx, k_gram_partial, grid, 256, 0, n, k1, k2, V, ldv, W, ldw, ctx->scratch, rps, sym);
+    GB_LAUNCH(ctx, k_gram_reduce, elem_grid(ctx, (long)k1 * k2), 256, 0, k1, k2, (int)nsplit, ctx->scratch,
+              a_dev, lda, sym);
+    return GCGE_GPU_OK;
+}
+
+// ---------------------------------------------------------------- linear combination X*C
+// Y[r, j] = alpha * sum_i X[r, i] C[i + j*ldc] + beta * Y[r, j]; tile 64 rows x 32 cols.
+__global__ void __launch_bounds__(256)
+k_lincomb(int n, int k1, int k2, const double *__restrict__ X, long ldx, const double *__restrict__ C, int ldc,
+          double alpha, double beta, double *__restrict__ Y, long ldy, int upper)
+{
+    __shared__ double Xs[64][33];
+    __shared__ double Cs[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const long r0 = (long)blockIdx.x * 64;
+    const int j0 = blockIdx.y * 32;
+    const int j = j0 + tx;
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    int iend = k1;
+    if (upper) iend = min(k1, j0 + 32);
+    for (int i0 = 0; i0 < iend; i0 += 32) {
+        for (int e = threadIdx.x; e < 64 * 32; e += 256) {
+            const int rr = e >> 5, cc = e & 31;
+            const long r = r0 + rr;
+            Xs[rr][cc] = (r < n && i0 + cc < k1) ? X[r * ldx + i0 + cc] : 0.0;
+        }
+        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+            const int ii = e & 31, cc = e >> 5;
+            Cs[ii][cc] = (i0 + ii < k1 && j0 + cc < k2) ? C[(i0 + ii) + (long)(j0 + cc) * ldc] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int ii = 0; ii < 32; ++ii) {
+            const double c = Cs[ii][tx];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[q] = fma(Xs[ty + 8 * q][ii], c, acc[q]);
+        }
+        __syncthreads();
+    }
+    if (j < k2) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const long r = r0 + ty + 8 * q;
+            if (r < n) {
+                double *y = Y + r * ldy + j;
+                *y = beta == 0.0 ? alpha * acc[q] : alpha * acc[q] + beta * *y;
+            }
+        }
+    }
+}
+
+extern "C" int gb_lincomb(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *X, long ldx,
+                          const double *C_dev, int ldc, double alpha, double beta, double *Y, long ldy,
+                          int upper)
+{
+    if (n <= 0 || k2 <= 0) return GCGE_GPU_OK;
+    if (k1 <= 0) return gb_axpby(ctx, n, k2, 0.0, Y, ldy, beta, Y, ldy);
+    dim3 grid(ceil_div_l(n, 64), (k2 + 31) / 32);
+    GB_PROF(ctx, GB_K_LINCOMB, 8.0 * n * k1 + (beta != 0.0 ? 16.0 : 8.0) * n * k2,
+            upper ? 1.0 * n * k1 * (k2 + 1) : 2.0 * n * k1 * k2);
+    GB_LAUNCH(ctx, k_lincomb, grid, 256, 0, n, k1, k2, X, ldx, C_dev, ldc, alpha, beta, Y, ldy, upper);
+    return GCGE_GPU_OK;
+}
+
+// Frobenius norm of a small column-major block (one block, fixed order)
+__global__ void k_frobenius(int m, int n, const double *a, int lda, double *out)
+{
+    __shared__ double sh[256];
+    double s = 0;
+    for (long t = threadIdx.x; t < (long)m * n; t += 256) {
+        const double v = a[(t % m) + (t / m) * lda];
+        s = fma(v, v, s);
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sqrt(sh[0]);
+}
+extern "C" int gb_frobenius(gcge_gpu_ctx *ctx, int m, int n, const double *a, int lda, double *out_dev)
+{
+    GB_LAUNCH(ctx, k_frobenius, 1, 256, 0, m, n, a, lda, out_dev);
+    return GCGE_GPU_OK;
+}
+
+// out[c] = src[idx[c]] (eigenvalues of the unlocked columns)
+__global__ void k_select(int k, const double *src, const int *idx, double *out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < k) out[c] = src[idx[c]];
+}
+extern "C" int gb_select(gcge_gpu_ctx *ctx, int k, const double *src, const int *idx, double *out)
+{
+    if (k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_select, (k + 127) / 128, 128, 0, k, src, idx, out);
+    return GCGE_GPU_OK;
+}
+
+// Y[:, c] = s[c] * X[:, c]
+__global__ void k_scale_cols(int n, int k, const double *__restrict__ X, long ldx, const double *__restrict__ s,
+                             double *Y, long ldy)
+{
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        Y[r * ldy + c] = s[c] * X[r * ldx + c];
+    }
+}
+extern "C" int gb_scale_cols(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, const double *s, double *Y,
+                             long ldy)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_scale_cols, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, s, Y, ldy);
+    return GCGE_GPU_OK;
+}

@@ -1,0 +1,43 @@
+/*
+ * gb_orth.h -- Cholesky-QR orthonormalisation workspace and entry, shared by
+ * the ABI (gb_api.cu) and the host driver (gb_solver.c).
+ */
+#ifndef GB_ORTH_H
+#define GB_ORTH_H
+
+#include "gb_internal.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int max_width, max_start;
+    double *T1;      /* n x ld1 block: B*W and the re-combined columns */
+    long ld1;
+    double *G;       /* Gram blocks: max(max_start, max_width) x max_width */
+    double *Tm;      /* max_width^2 coefficient matrix */
+    double *chol_work;
+    double *small;   /* norms */
+    int *kept_dev;
+} gb_orth_ws;
+
+int  gb_orth_ws_alloc(gcge_gpu_ctx *ctx, gb_orth_ws *ws, int n, int max_width, int max_start);
+void gb_orth_ws_free(gb_orth_ws *ws);
+
+/* B-orthonormalise V[:, start:*end) (row-major block, ld ldv) against
+ * V[:, 0:start) and itself: up to max_reorth_time block projection passes (a
+ * third only when the second still removed more than 1e-10 of the first), then
+ * Cholesky-QR twice with deflation; kept columns are packed at start, *end
+ * shrinks by the number dropped. */
+int gb_orthonormalize(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int *end,
+                      const gcge_gpu_mat *B, int max_reorth_time, double zero_tol, gb_orth_ws *ws);
+
+/* column-major host n x k  <->  row-major device block columns */
+int gb_upload_cols(gcge_gpu_ctx *ctx, int n, int k, const double *host, double *d, long ld);
+int gb_download_cols(gcge_gpu_ctx *ctx, int n, int k, const double *d, long ld, double *host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

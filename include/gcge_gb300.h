@@ -1,0 +1,199 @@
+/*
+ * gcge_gb300.h -- C ABI of the GB300-native GCGE CSR eigensolver path.
+ *
+ * One process, one GPU (sm_103a). All entry points are plain C: opaque handles,
+ * host pointers and sizes, an int status (GCGE_GPU_OK = 0 on success). No CPU
+ * fallback exists: without a usable CUDA device every call fails with
+ * GCGE_GPU_ERR_CUDA.
+ *
+ * The entry points fall in four groups, each replacing a reference interface
+ * (file:line inside the GCGE-1.0 project):
+ *
+ *  1. Device data.  GCGE_GPU_MatCreate uploads a CSR matrix in the reference's
+ *     CSR_MAT layout (app/csr/gcge_app_csr.h:27-40); GCGE_GPU_MultiVecCreate
+ *     allocates a multivector (the role of ops->MultiVecCreateByMat,
+ *     src/gcge_ops.h:59). Multivectors live in HBM as row-major n x ncols
+ *     blocks (each row of the block contiguous).
+ *  2. Block operations with the semantics of the GCGE_OPS multivector members
+ *     (src/gcge_ops.h:57-86): MatDotMultiVec, MultiVecAxpby, MultiVecLinearComb,
+ *     MultiVecInnerProd, MultiVecSwap. Column ranges are half open
+ *     [start[i], end[i]); index 0 refers to the first multivector argument,
+ *     index 1 to the second; dense coefficient arrays are column major with an
+ *     explicit leading dimension, as in the reference.
+ *  3. The plug-in table. GCGE_GPU_SetOps fills a GCGE_OPS table
+ *     (src/gcge_ops.h:29-215) with device implementations, so GCGE's own
+ *     GCGE_SOLVER_* calls run on the GPU. See gcge_gb300_ops.h.
+ *  4. The GPU-native solver. GCGE_GPU_Solve runs the whole GCG iteration of
+ *     GCGE_Solve (src/gcge_eigsol.c:65-542) on the device with the GCGE_PARA
+ *     parameters (src/gcge_para.h:41-103); GCGE_GPU_SolveHost does the same from
+ *     host CSR arrays, the counterpart of GCGE_CSR_Solver_Init + GCGE_SOLVER_Solve
+ *     (app/csr/gcge_app_csr.c:92-124, src/gcge_solver.c:98-101).
+ */
+#ifndef GCGE_GB300_H
+#define GCGE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define GCGE_GPU_OK            0
+#define GCGE_GPU_ERR_ARG       1   /* invalid argument (sizes, ranges, NULL)            */
+#define GCGE_GPU_ERR_CUDA      2   /* CUDA runtime error (no device, launch failure)    */
+#define GCGE_GPU_ERR_NOMEM     3   /* device allocation failed                          */
+#define GCGE_GPU_ERR_CSR       4   /* malformed CSR (row pointers, column range)        */
+#define GCGE_GPU_ERR_NONFINITE 5   /* NaN/Inf met in a reduction or the small eigensolve */
+#define GCGE_GPU_ERR_BREAKDOWN 6   /* orthogonalisation lost every column               */
+#define GCGE_GPU_ERR_EIGSOLVE  7   /* projected eigensolve did not converge             */
+
+typedef struct gcge_gpu_ctx gcge_gpu_ctx;  /* device, stream, reduction scratch  */
+typedef struct gcge_gpu_mat gcge_gpu_mat;  /* CSR matrix resident in HBM         */
+typedef struct gcge_gpu_mv  gcge_gpu_mv;   /* row-major multivector in HBM       */
+
+/* Context: binds a CUDA device and creates the stream every call is ordered on. */
+int  GCGE_GPU_Init(int device, gcge_gpu_ctx **ctx);
+int  GCGE_GPU_Finalize(gcge_gpu_ctx *ctx);
+/* The first error any call on this context met (sticky), then cleared. The
+ * GCGE_OPS table members return void as in the reference, so they record their
+ * failures here. */
+int  GCGE_GPU_GetLastError(gcge_gpu_ctx *ctx);
+const char *GCGE_GPU_ErrorString(int status);
+int  GCGE_GPU_Synchronize(gcge_gpu_ctx *ctx);
+
+/* ---- 1. device data ---- */
+
+/* Upload an n x n CSR matrix (RowPtr[n+1], KCol[nnz], Entries[nnz], as CSR_MAT,
+ * app/csr/gcge_app_csr.h:27-40). keep_fp32 != 0 also keeps an FP32 copy of the
+ * values for the mixed-precision inner solve. The structure is validated on the
+ * host first (GCGE_GPU_ERR_CSR). */
+int  GCGE_GPU_MatCreate(gcge_gpu_ctx *ctx, int n, const int *rowptr, const int *col,
+                        const double *val, int keep_fp32, gcge_gpu_mat **A);
+/* Replace the values (same pattern); refreshes the FP32 copy if kept. */
+int  GCGE_GPU_MatSetValues(gcge_gpu_mat *A, const double *val);
+int  GCGE_GPU_MatDestroy(gcge_gpu_mat *A);
+int  GCGE_GPU_MatGetSize(const gcge_gpu_mat *A, int *n, int *nnz);
+
+int  GCGE_GPU_MultiVecCreate(gcge_gpu_ctx *ctx, int n, int ncols, gcge_gpu_mv **mv);
+int  GCGE_GPU_MultiVecDestroy(gcge_gpu_mv *mv);
+/* Host <-> device copies of columns [col0, col0+ncols); host arrays are column
+ * major n x ncols (leading dimension n), the reference's vector-per-column view. */
+int  GCGE_GPU_MultiVecUpload(gcge_gpu_mv *mv, int col0, int ncols, const double *host);
+int  GCGE_GPU_MultiVecDownload(const gcge_gpu_mv *mv, int col0, int ncols, double *host);
+/* Fill columns [start, start+nvec) with uniform [0,1) values of the counter hash
+ * (seed, column*n + row); ops->MultiVecSetRandomValue, src/gcge_ops.h:66. */
+int  GCGE_GPU_MultiVecSetRandomValue(gcge_gpu_mv *mv, int start, int nvec, unsigned long long seed);
+
+/* ---- 2. block operations (semantics of src/gcge_ops.c:115-300) ---- */
+
+/* y(:, start[1]:end[1]) = A x(:, start[0]:end[0]); ops->MatDotMultiVec,
+ * src/gcge_ops.h:67 (default loop src/gcge_ops.c:115-129). */
+int  GCGE_GPU_MatDotMultiVec(const gcge_gpu_mat *A, const gcge_gpu_mv *x, gcge_gpu_mv *y,
+                             const int *start, const int *end);
+/* y(:, s1:e1) = a x(:, s0:e0) + b y(:, s1:e1), with CSR_VecAxpby's special cases
+ * (a == 0: y = b y; b == 0: y = a x); ops->MultiVecAxpby, src/gcge_ops.h:69. */
+int  GCGE_GPU_MultiVecAxpby(double a, const gcge_gpu_mv *x, double b, gcge_gpu_mv *y,
+                            const int *start, const int *end);
+/* y(:, s1:e1) = x(:, s0:e0) * a, a column major (e0-s0) x (e1-s1) host array with
+ * leading dimension lda; ops->MultiVecLinearComb, src/gcge_ops.h:74. */
+int  GCGE_GPU_MultiVecLinearComb(const gcge_gpu_mv *x, gcge_gpu_mv *y, const int *start,
+                                 const int *end, const double *a, int lda);
+/* a(0:e0-s0, 0:e1-s1) = V(:, s0:e0)^T W(:, s1:e1) into a host array with leading
+ * dimension lda; is_sym "sym" computes the upper triangle and mirrors it.
+ * ops->MultiVecInnerProd, src/gcge_ops.h:77 (src/gcge_ops.c:198-281). */
+int  GCGE_GPU_MultiVecInnerProd(const gcge_gpu_mv *V, const gcge_gpu_mv *W, double *a,
+                                const char *is_sym, const int *start, const int *end, int lda);
+/* Exchange V1(:, s0:e0) and V2(:, s1:e1) (data, not handles); ops->MultiVecSwap,
+ * src/gcge_ops.h:79. */
+int  GCGE_GPU_MultiVecSwap(gcge_gpu_mv *V1, gcge_gpu_mv *V2, const int *start, const int *end);
+
+/* Block CG on A W = RHS for k columns, GCGE_BCG (src/gcge_cg.c:137-302): W (initial
+ * guess in, solution out) and RHS (overwritten by the residual) are the column
+ * ranges [w_start, w_start+k) and [r_start, r_start+k). precision 0: FP64;
+ * 1: FP32 vectors and FP32 matrix values with FP64-accumulated dot products
+ * (requires keep_fp32 on A). */
+int  GCGE_GPU_BCG(const gcge_gpu_mat *A, gcge_gpu_mv *RHS, int r_start, gcge_gpu_mv *W,
+                  int w_start, int k, int cg_max_it, double cg_rate, int precision);
+
+/* B-orthonormalise W(:, start:*end) against W(:, 0:start) (already B-orthonormal)
+ * and itself: block projection passes, then Cholesky-QR twice with deflation of
+ * dependent columns (kept columns are packed to the front, *end shrinks). Role of
+ * GCGE_StableMultiOrthonormalization, src/gcge_orthogonal.c:1833-1877. B may be NULL. */
+int  GCGE_GPU_Orthonormalize(gcge_gpu_mv *W, int start, int *end, const gcge_gpu_mat *B,
+                             int max_reorth_time, double orth_zero_tol);
+
+/* ---- 4. GPU-native solver ---- */
+
+/* GCGE_PARA members that drive the solve (src/gcge_para.h:41-103, defaults of
+ * GCGE_PARA_Create src/gcge_para.c:25-99), plus precision and the seed of the
+ * initial vectors. */
+typedef struct {
+    int    nev;               /* wanted eigenpairs                                   */
+    int    block_size;        /* 0 -> nev                                             */
+    int    ev_max_it;         /* 30                                                   */
+    int    cg_max_it;         /* 20                                                   */
+    int    max_reorth_time;   /* 3                                                    */
+    int    dirichlet_boundary;/* zero Dirichlet rows of the initial X                  */
+    int    given_init_evec;   /* 1: evec holds the initial vectors                    */
+    double ev_tol;            /* 1e-8                                                 */
+    double cg_rate;           /* 1e-2                                                 */
+    double orth_zero_tol;     /* 1e-16 (+DBL_EPSILON)                                 */
+    char   conv_type[4];      /* "R", "A", "O" as the reference; "BR":
+                                 ||Ax - lambda Bx|| / (|lambda| ||Bx||)               */
+    int    precision;         /* 0 plain FP64; 1 mixed (FP32 inner block CG)          */
+    unsigned long long seed;  /* counter-hash seed of the initial vectors             */
+    int    print_level;       /* 0 silent; 1 one line per iteration (reference format)*/
+} gcge_gpu_params;
+
+typedef struct {
+    int    num_iter;          /* outer GCG iterations (para->num_iter)                 */
+    int    num_unlock;        /* eigenpairs still above ev_tol                         */
+    double max_res, min_res, sum_res;
+    double res[8];            /* unused, reserved                                      */
+    double solve_ms;          /* device time of the solve (CUDA events)                */
+    double phase_ms[9];       /* GCGE_PART_TIME slots (src/gcge_statistics.h:23-33):
+                                 x_axpy, x_orth, p_axpy, p_orth, w_line, w_orth,
+                                 rr_mat, rr_eigen, conv                                */
+    long long kernel_launches;/* kernels this library launched during the solve        */
+    long long spmm_calls;     /* CSR SpMM launches (FP64 + FP32)                       */
+} gcge_gpu_stats;
+
+void GCGE_GPU_ParamsDefault(gcge_gpu_params *p);
+
+/* Solve A x = lambda B x for the nev smallest eigenpairs with device-resident A,
+ * B (B may be NULL: B = I). eval: host array [nev]; evec: multivector with at
+ * least nev columns (read when given_init_evec = 1, holds the eigenvectors on exit). */
+int  GCGE_GPU_Solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B,
+                    const gcge_gpu_params *p, double *eval, gcge_gpu_mv *evec,
+                    gcge_gpu_stats *stats);
+
+/* Host-buffer entry: uploads the CSR arrays, solves, downloads eval[nev] and
+ * evec (column major n x nev, leading dimension n), frees the device copies. */
+int  GCGE_GPU_SolveHost(gcge_gpu_ctx *ctx, int n,
+                        const int *A_rowptr, const int *A_col, const double *A_val,
+                        const int *B_rowptr, const int *B_col, const double *B_val,
+                        const gcge_gpu_params *p, double *eval, double *evec,
+                        gcge_gpu_stats *stats);
+
+/* Number of this library's kernel launches on the context so far (a counter the
+ * host wrappers increment at every launch). Instrumentation with no counterpart
+ * in the reference. */
+long long GCGE_GPU_LaunchCount(const gcge_gpu_ctx *ctx);
+
+/* Profiling mode (instrumentation, no counterpart in the reference): while on,
+ * every launch of the hot kernels is bracketed by CUDA events on the context's
+ * stream and attributed to a class with its algorithmic bytes and flops.
+ * Classes, in order: 0 CSR SpMM FP64, 1 CSR SpMM FP32, 2 Gram V^T W,
+ * 3 linear combination X*C, 4 block-CG vector updates and dots, 5 AXPBY/copies,
+ * 6 small dense GEMM, 7 small dense eigensolve, 8 per-column reductions.
+ * ProfileRead fills up to nclass entries of each non-NULL array and returns
+ * the number of classes (reset != 0 zeroes the totals afterwards). */
+int  GCGE_GPU_ProfileEnable(gcge_gpu_ctx *ctx, int on);
+int  GCGE_GPU_ProfileRead(gcge_gpu_ctx *ctx, int nclass, double *ms, long long *launches,
+                          double *bytes, double *flops, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

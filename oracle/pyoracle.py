@@ -83,8 +83,11 @@ class Oracle(_Lib):
     def __init__(self):
         path = os.path.join(HERE, "libgcge_oracle.so")
         if not os.path.exists(path):
-            import build
-            build.build_oracle()
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("gcge_oracle_build", os.path.join(HERE, "build_oracle.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build_oracle()
         super().__init__(path, "gcge_oracle_solve")
         L = self.lib
         L.gcge_oracle_csr_matmultivec.argtypes = [C.c_int, C.c_int, _I, _I, _D, _D, _D]

@@ -1,7 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the compiled GCGE-1.0
 reference (oracle/_ref). Run here, where the reference source tree exists:
 
-    python oracle/build.py && python tests/golden/make_golden.py
+    python oracle/build_oracle.py && python tests/golden/make_golden.py
 
 Outputs:
 * fem33_A.npz / fem33_M.npz: the reference's own FEM test pencil (test/data/A_5.txt,
@@ -51,7 +51,7 @@ def cases():
 def main():
     ref = pyoracle.reference()
     if ref is None:
-        raise SystemExit("oracle/_ref/libgcge_ref.so is missing: run python oracle/build.py here")
+        raise SystemExit("oracle/_ref/libgcge_ref.so is missing: run python oracle/build_oracle.py here")
     A5 = P.read_csr_text(os.path.join(REF_DATA, "A_5.txt"))
     M5 = P.read_csr_text(os.path.join(REF_DATA, "M_5.txt"))
     save_csr(os.path.join(HERE, "fem33_A.npz"), A5)
