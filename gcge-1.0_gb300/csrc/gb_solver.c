@@ -517,38 +517,52 @@ int GCGE_GPU_Solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat 
     ph_collect(g);
 
     /* ---- [X, P, W] loop (src/gcge_eigsol.c:396-528) ---- */
-    while (g->num_unlock > 0 && g->num_iter < g->p.ev_max_it) {
-        TRY(compute_p(g));
-        TRY(x_to_v(g));
-        ph_begin(g, PH_W_LINE);
-        TRY(compute_w(g));
-        ph_end(g);
-        g->last_dim_xpw = g->dim_xpw;
-        g->dim_xpw = g->dim_xp + g->unconv_bs;
-        ph_begin(g, PH_W_ORTH);
-        TRY(gb_orthonormalize(ctx, n, g->V, g->ldv, g->dim_xp, &g->dim_xpw, B, g->p.max_reorth_time, g->zero_tol,
-                              &g->ows));
-        ph_end(g);
-        ph_begin(g, PH_RR_MAT);
-        TRY(rr_matrix(g));
-        ph_end(g);
-        ph_begin(g, PH_RR_EIGEN);
-        TRY(rr_eig(g));
-        ph_end(g);
-        ph_begin(g, PH_X_AXPY);
-        TRY(compute_x(g));
-        ph_end(g);
+    for (;;) {
+        while (g->num_unlock > 0 && g->num_iter < g->p.ev_max_it) {
+            TRY(compute_p(g));
+            TRY(x_to_v(g));
+            ph_begin(g, PH_W_LINE);
+            TRY(compute_w(g));
+            ph_end(g);
+            g->last_dim_xpw = g->dim_xpw;
+            g->dim_xpw = g->dim_xp + g->unconv_bs;
+            ph_begin(g, PH_W_ORTH);
+            TRY(gb_orthonormalize(ctx, n, g->V, g->ldv, g->dim_xp, &g->dim_xpw, B, g->p.max_reorth_time, g->zero_tol,
+                                  &g->ows));
+            ph_end(g);
+            ph_begin(g, PH_RR_MAT);
+            TRY(rr_matrix(g));
+            ph_end(g);
+            ph_begin(g, PH_RR_EIGEN);
+            TRY(rr_eig(g));
+            ph_end(g);
+            ph_begin(g, PH_X_AXPY);
+            TRY(compute_x(g));
+            ph_end(g);
+            ph_begin(g, PH_CONV);
+            TRY(check_conv(g));
+            ph_end(g);
+            ph_collect(g);
+            /* CheckEvalMultiplicity on the eigenvalues check_conv brought back; ComputeX
+             * only forms nev columns, so the new dim_x is first used by ComputeP */
+            g->last_dim_x = g->dim_x;
+            {
+                const int ldm = g->dim_xpw, iu = g->max_dim_x < ldm ? g->max_dim_x : ldm;
+                g->dim_x = check_multiplicity(nev, iu, g->eval_h);
+            }
+        }
+        /* The reference only re-checks pairs that were unconverged, so a pair that
+         * converged early can drift above the tolerance in later iterations. Verify
+         * every pair once on exit and keep iterating on the ones above it. */
+        if (g->num_unlock > 0 || g->num_iter >= g->p.ev_max_it) break;
+        g->num_unlock = nev;
+        for (int i = 0; i < nev; ++i) g->unlock_h[i] = i;
+        g->num_iter -= 1;   /* the verification is not an iteration */
         ph_begin(g, PH_CONV);
         TRY(check_conv(g));
         ph_end(g);
         ph_collect(g);
-        /* CheckEvalMultiplicity on the eigenvalues check_conv brought back; ComputeX
-         * only forms nev columns, so the new dim_x is first used by ComputeP */
-        g->last_dim_x = g->dim_x;
-        {
-            const int ldm = g->dim_xpw, iu = g->max_dim_x < ldm ? g->max_dim_x : ldm;
-            g->dim_x = check_multiplicity(nev, iu, g->eval_h);
-        }
+        if (g->num_unlock == 0) break;
     }
 
     CTRY(cudaEventRecord(e1, ctx->stream));

@@ -1,0 +1,74 @@
+"""The C-ABI boundary without a GPU: the library loads, exports every entry point
+declared in include/*.h, fails loudly when no device is present, and the
+GCGE_OPS layout restated in include/gcge_gb300_ops.h matches the reference's."""
+import ctypes as C
+import os
+import subprocess
+
+import pytest
+
+import gcge_gb300 as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.environ.get("GCGE_REFERENCE_ROOT", "/root/reference")
+
+
+def has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def test_library_exports_every_declared_symbol():
+    L = G.load()
+    declared = G.declared_symbols()
+    assert len(declared) >= 28
+    missing = [s for s in declared if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_error_strings():
+    L = G.load()
+    for st in range(8):
+        assert L.GCGE_GPU_ErrorString(st)
+    assert L.GCGE_GPU_ErrorString(99) == b"unknown status"
+
+
+@pytest.mark.skipif(has_gpu(), reason="a CUDA device is present")
+def test_init_fails_loudly_without_gpu():
+    with pytest.raises(G.GcgeGpuError) as e:
+        G.Context(0)
+    assert e.value.status == 2
+
+
+def test_null_arguments_rejected():
+    L = G.load()
+    assert L.GCGE_GPU_Init(0, None) == 1
+    assert L.GCGE_GPU_MatCreate(None, 10, None, None, None, 0, None) == 1
+    assert L.GCGE_GPU_SetOps(None, None) == 1
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree absent")
+def test_ops_layout_matches_reference(tmp_path):
+    cmd = ["gcc", "-std=gnu99", "-c", "-o", str(tmp_path / "x.o"), "-include", os.path.join(ROOT, "oracle", "ref_config.h"),
+           "-I" + os.path.join(REF, "src"), "-I" + os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "abi", "ops_layout_check.c")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_python_structs_match_c_headers():
+    """ctypes mirrors of gcge_gpu_params / gcge_gpu_stats have the C sizes."""
+    src = tmp = None
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "s.c")
+        open(src, "w").write('#include <stdio.h>\n#include "gcge_gb300.h"\nint main(){printf("%zu %zu\\n",'
+                             ' sizeof(gcge_gpu_params), sizeof(gcge_gpu_stats));return 0;}\n')
+        exe = os.path.join(d, "s")
+        subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), src, "-o", exe])
+        a, b = map(int, subprocess.check_output([exe]).split())
+    assert C.sizeof(G.Params) == a
+    assert C.sizeof(G.Stats) == b
