@@ -565,3 +565,34 @@ extern "C" int gb_scale_cols(gcge_gpu_ctx *ctx, int n, int k, const double *X, l
     GB_LAUNCH(ctx, k_scale_cols, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, s, Y, ldy);
     return GCGE_GPU_OK;
 }
+
+// Gram V^T W with caller-provided partial-sum storage and stream (no context,
+// no allocation): the launcher behind the allocation-free entry point. part
+// must hold part_cap doubles; returns GCGE_GPU_ERR_ARG when k1*k2 does not fit
+// at least one row split.
+extern "C" int gb_gram_fixed_scratch(cudaStream_t stream, int num_sms, int n, int k1, int k2, const double *V,
+                                     long ldv, const double *W, long ldw, double *a_dev, int lda, int sym,
+                                     double *part, size_t part_cap)
+{
+    const int ti = (k1 + 31) / 32, tj = (k2 + 31) / 32;
+    int tiles = sym ? ti * (ti + 1) / 2 : ti * tj;
+    if (tiles < 1) tiles = 1;
+    long nsplit = ((long)num_sms * 4) / tiles;
+    const long max_split = (n + 255) / 256;
+    if (nsplit > max_split) nsplit = max_split;
+    const long fit = (long)(part_cap / ((size_t)k1 * k2));
+    if (nsplit > fit) nsplit = fit;
+    if (nsplit < 1) return GCGE_GPU_ERR_ARG;
+    long rps = ((n + nsplit - 1) / nsplit + 31) / 32 * 32;
+    if (rps < 32) rps = 32;
+    nsplit = (n + rps - 1) / rps;
+    if (nsplit < 1) nsplit = 1;
+    dim3 grid(ti, tj, (unsigned)nsplit);
+    k_gram_partial<<<grid, 256, 0, stream>>>(n, k1, k2, V, ldv, W, ldw, part, rps, sym);
+    if (cudaGetLastError() != cudaSuccess) return GCGE_GPU_ERR_CUDA;
+    long g = ((long)k1 * k2 + 255) / 256;
+    if (g > (long)num_sms * 16) g = (long)num_sms * 16;
+    k_gram_reduce<<<(int)(g > 0 ? g : 1), 256, 0, stream>>>(k1, k2, (int)nsplit, part, a_dev, lda, sym);
+    if (cudaGetLastError() != cudaSuccess) return GCGE_GPU_ERR_CUDA;
+    return GCGE_GPU_OK;
+}

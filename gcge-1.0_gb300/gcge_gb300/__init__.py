@@ -96,6 +96,7 @@ def load():
         "GCGE_GPU_OpsMultiVecBlock": (_I, [_P, C.POINTER(_P), C.POINTER(_I)]),
         "GCGE_GPU_ProfileEnable": (_I, [_P, _I]),
         "GCGE_GPU_ProfileRead": (_I, [_P, _I, _P, _P, _P, _P, _I]),
+        "GCGE_GPU_InnerProdNoAlloc": (_I, [_I, _I, _I, _P, C.c_long, _P, C.c_long, _P, _I, _I, _P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -193,6 +193,26 @@ int  GCGE_GPU_ProfileEnable(gcge_gpu_ctx *ctx, int on);
 int  GCGE_GPU_ProfileRead(gcge_gpu_ctx *ctx, int nclass, double *ms, long long *launches,
                           double *bytes, double *flops, int reset);
 
+/* ---- allocation-free Gram product (no counterpart in the reference) ----
+ *
+ * For callers that own all device memory through their own pool or arena and
+ * may not call cudaMalloc / cudaFree (those calls can synchronise the device and
+ * would take memory the pool has already claimed). Computes the Gram block of
+ * GCGE_GPU_MultiVecInnerProd, a(0:k1, 0:k2) = V^T W ("sym": upper triangle
+ * computed and mirrored), on caller memory and allocates nothing:
+ *   V, W   device pointers to row-major blocks, element (r, c) at V[r*ldv + c]
+ *          (the multivector layout of this library), n rows, k1 / k2 columns;
+ *   a      device pointer, column major with leading dimension lda >= k1;
+ *   stream a cudaStream_t (NULL: the default stream); the call is asynchronous.
+ * Partial sums go to a fixed 8 MiB device array inside the library (held by
+ * every GPU that loads it, until exit), so k1*k2 may be at most 262,144.
+ * Larger sizes are rejected with GCGE_GPU_ERR_ARG. The first call on a device
+ * looks up the array's device address with that device current; make that
+ * first call before any stream capture. All calls share the array and it keeps
+ * the last call's contents; calls that overlap on the GPU race on it. */
+int  GCGE_GPU_InnerProdNoAlloc(int n, int k1, int k2, const double *V, long ldv, const double *W,
+                               long ldw, double *a, int lda, int sym, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
