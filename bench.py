@@ -148,35 +148,41 @@ def check_solution(A, B, ev, X, exact):
     return float(r.max()), float(np.max(np.abs(ev - exact) / exact))
 
 
-def cpu_sample(workload_full_n, gpu_iters=None, threads=1):
-    """Bounded CPU run: the oracle port (restatement of the reference CSR path, scalar C;
-    OpenBLAS limited to `threads` for the small dense calls) on the same pencil family at
-    ne = 24 (n = 12,167), 50 eigenpairs, block 64, residual <= 1e-8. Its wall time is
-    scaled to the full workload by the row ratio (every per-iteration cost of the path is
-    linear in n at fixed nev) and, when known, by the ratio of GCG iterations."""
+def cpu_sample(workload_full_n, gpu_iters=None, threads=1, ne=32):
+    """Bounded CPU run of the oracle port (restatement of the reference CSR path, scalar C;
+    OpenBLAS limited to `threads` for the small dense calls) on the same pencil family at a
+    reduced mesh (ne = 32: n = 29,791), 50 eigenpairs, block 64, residual <= 1e-8: the solve
+    is run for 2 and for 6 outer GCG iterations; t(2) covers the set-up and first steps and
+    (t(6) - t(2)) / 4 is the time of one outer iteration. The estimate for the full workload
+    is t(2) + per-iteration time x (iterations - 2), with the iteration count the GPU solve
+    needed (else 40), scaled by the row ratio (every per-iteration cost of the path is
+    linear in n at fixed nev; the small sample stays in cache, so this under-estimates)."""
     code = r"""
 import json, os, sys, time
 sys.path.insert(0, %r); sys.path.insert(0, %r)
 import pyoracle
 from gcge_gb300 import problems as P
-A, B = P.fem_q1_cube(24)
+A, B = P.fem_q1_cube(%d)
 o = pyoracle.Oracle()
-p = o.params(nev=50, block_size=64, ev_max_it=400, conv_type="BR", init_rng=1, seed=7)
-t = time.time(); ev, X, st = o.solve(A, B, p); w = time.time() - t
-print(json.dumps({"wall": w, "iters": st.num_iter, "n": A.n, "unlock": st.num_unlock}))
-""" % (os.path.join(ROOT, "gcge-1.0_gb300"), os.path.join(ROOT, "oracle"))
+out = {"n": A.n}
+for it in (2, 6):
+    p = o.params(nev=50, block_size=64, ev_max_it=it, conv_type="BR", init_rng=1, seed=7)
+    t = time.time(); ev, X, st = o.solve(A, B, p); out["t%%d" %% it] = time.time() - t
+print(json.dumps(out))
+""" % (os.path.join(ROOT, "gcge-1.0_gb300"), os.path.join(ROOT, "oracle"), ne)
     env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads))
-    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
     if r.returncode != 0:
         raise RuntimeError("cpu sample failed: " + r.stderr[-2000:])
     d = json.loads(r.stdout.strip().splitlines()[-1])
+    per_it = max(d["t6"] - d["t2"], 0.0) / 4.0
+    iters = gpu_iters if gpu_iters else 40
     scale_n = workload_full_n / d["n"]
-    scale_it = (gpu_iters / d["iters"]) if gpu_iters else 1.0
-    est = d["wall"] * scale_n * scale_it
-    sample = ("oracle port (C restatement of the reference CSR GCGE), full solve of the Q1 cube at ne=24 "
-              "(n=%d, nev=50, block 64, BR<=1e-8): %.2f s wall, %d GCG iterations; scaled by n ratio %.2f%s"
-              % (d["n"], d["wall"], d["iters"], scale_n,
-                 (" and iteration ratio %d/%d" % (gpu_iters, d["iters"])) if gpu_iters else ""))
+    est = (d["t2"] + per_it * max(iters - 2, 0)) * scale_n
+    sample = ("oracle port (C restatement of the reference CSR GCGE) on the Q1 cube at ne=%d (n=%d, nev=50, "
+              "block 64): 2 outer iterations %.2f s, 6 outer iterations %.2f s wall; full solve estimated as "
+              "t2 + %.3f s/iteration x (%d-2), scaled by the row ratio %.1f" %
+              (ne, d["n"], d["t2"], d["t6"], per_it, iters, scale_n))
     return est, sample
 
 

@@ -40,29 +40,29 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
     } while (0)
 
 struct bcg_state {
-    double *rho1, *rho2, *err, *ptw, *part;
+    double *rho1, *rho2, *err, *ptw, *part, *alpha, *beta;
     int *nact;
 };
 
-// p = r + beta p on active columns (beta = 0 on the first round: p = r)
+// warp-per-row loop over an n x k block: lanes walk the columns of one row
+#define ROWS_BY_WARP(n, r)                                                             \
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (n);         \
+         r += ((long)gridDim.x * blockDim.x) >> 5)
+
+// p = r + beta p on active columns (beta = 0 on the first round: p = r);
+// beta[c] = rho2[c] / rho1[c] was formed once per column by k_finalize
 template <typename T>
 __global__ void k_pupdate(int n, int k, const T *__restrict__ R, T *__restrict__ P, long ld,
-                          const double *__restrict__ rho1, const double *__restrict__ rho2,
-                          const int *__restrict__ nact, int first)
+                          const double *__restrict__ beta, const int *__restrict__ nact, int first)
 {
-    const int ka = *nact;
+    const int ka = min(*nact, k);
     if (ka <= 0) return;
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
-        if (c >= ka) continue;
-        if (first) {
-            P[r * ld + c] = R[r * ld + c];
-        } else {
-            const T beta = (T)(rho2[c] / rho1[c]);
-            P[r * ld + c] = R[r * ld + c] + beta * P[r * ld + c];
-        }
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    {
+        const T *rr = R + r * ld;
+        T *pr = P + r * ld;
+        for (int c = lane; c < ka; c += 32) pr[c] = first ? rr[c] : rr[c] + (T)beta[c] * pr[c];
     }
 }
 
@@ -102,7 +102,7 @@ k_dot_partial(int n, int k, const T *__restrict__ A, const T *__restrict__ B, lo
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_xr_update(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restrict__ P,
-            const T *__restrict__ W, long ld, const double *__restrict__ rho2, const double *__restrict__ ptw,
+            const T *__restrict__ W, long ld, const double *__restrict__ alpha,
             const int *__restrict__ nact, double *__restrict__ part)
 {
     __shared__ double sh[8][33];
@@ -112,8 +112,7 @@ k_xr_update(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restr
     const long r0 = (long)blockIdx.x * RED_ROWS, r1 = min((long)n, r0 + RED_ROWS);
     double s = 0;
     if (c < k && c < ka) {
-        const double ad = rho2[c] / ptw[c];
-        const T a = (T)ad;
+        const T a = (T)alpha[c];
         long r = r0 + ty;
         while (r < r1) {
             T run = 0;
@@ -139,15 +138,16 @@ k_xr_update(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restr
     }
 }
 
-// ptw[c] = sum of partials for active c
+// ptw[c] = sum of partials for active c, and alpha[c] = rho2[c] / ptw[c]
 __global__ void k_sum_active(int nblk, int k, const double *__restrict__ part, const int *__restrict__ nact,
-                             double *__restrict__ out)
+                             double *__restrict__ out, const double *__restrict__ rho2, double *__restrict__ alpha)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k || c >= *nact) return;
     double s = 0;
     for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
     out[c] = s;
+    alpha[c] = rho2[c] / s;
 }
 
 // initial residual norms: rho2 = sum partials, err = sqrt(rho2), nact = k
@@ -165,7 +165,7 @@ __global__ void k_init_state(int nblk, int k, const double *__restrict__ part, d
 
 // end of a round: rho1 = rho2, rho2 = new r.r (active columns); recount over all columns
 __global__ void k_finalize(int nblk, int k, const double *__restrict__ part, double *rho1, double *rho2,
-                           const double *__restrict__ err, int *nact, double rate)
+                           const double *__restrict__ err, int *nact, double rate, double *beta)
 {
     __shared__ int cnt;
     const int ka = *nact;
@@ -177,6 +177,7 @@ __global__ void k_finalize(int nblk, int k, const double *__restrict__ part, dou
             for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
             rho1[c] = rho2[c];
             rho2[c] = s;
+            beta[c] = s / rho1[c];   // the next round's beta (src/gcge_cg.c:645)
         }
         const double lerr = sqrt(fabs(rho2[c]));
         if (lerr / err[c] >= rate) atomicAdd(&cnt, 1);
@@ -188,12 +189,18 @@ __global__ void k_finalize(int nblk, int k, const double *__restrict__ part, dou
 // X += (double) D
 __global__ void k_add_f2d(int n, int k, const float *__restrict__ D, long ldd, double *__restrict__ X, long ldx)
 {
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
-        X[r * ldx + c] += (double)D[r * ldd + c];
-    }
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) X[r * ldx + c] += (double)D[r * ldd + c];
+}
+
+// blocks of 8 warps for a warp-per-row loop, capped at 16 blocks per SM
+static int row_grid(gcge_gpu_ctx *ctx, long rows)
+{
+    long g = (rows + 7) / 8, cap = (long)ctx->num_sms * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
 }
 
 static int elem_grid(gcge_gpu_ctx *ctx, long total)
@@ -210,7 +217,7 @@ extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
     size_t vec = precision ? sizeof(float) : sizeof(double);
     size_t nblk = (size_t)cdiv(n > 0 ? n : 1, RED_ROWS);
     size_t blocks = 4 * (size_t)n * ldk * vec;  // R, X, P, W
-    size_t state = (4 * (size_t)k + nblk * (size_t)k + 8) * sizeof(double) + 64;
+    size_t state = (6 * (size_t)k + nblk * (size_t)k + 8) * sizeof(double) + 64;
     return blocks + state + 16 * 256;   // every sub-buffer is aligned to 256 bytes (10 of them)
 }
 
@@ -223,8 +230,7 @@ static int bcg_rounds(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, T *R, T *X, T *P
     const double es = sizeof(T);
     for (int it = 1; it < a->max_it; ++it) {
         GB_PROF(ctx, GB_K_BCGVEC, 3.0 * es * n * k, 2.0 * n * k);
-        GB_LAUNCH(ctx, k_pupdate<T>, elem_grid(ctx, (long)n * k), 256, 0, n, k, R, P, ld, s->rho1, s->rho2,
-                  s->nact, it == 1);
+        GB_LAUNCH(ctx, k_pupdate<T>, row_grid(ctx, n), 256, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
         int st;
         if (sizeof(T) == sizeof(double))
             st = gb_spmm(ctx, A, (const double *)P, ld, (double *)W, ld, k, 1.0, nullptr, 0.0, s->nact);
@@ -233,10 +239,10 @@ static int bcg_rounds(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, T *R, T *X, T *P
         if (st) return st;
         GB_PROF(ctx, GB_K_BCGVEC, 2.0 * es * n * k, 2.0 * n * k);
         GB_LAUNCH(ctx, k_dot_partial<T>, rgrid, 256, 0, n, k, P, W, ld, s->nact, s->part);
-        GB_LAUNCH(ctx, k_sum_active, (k + 127) / 128, 128, 0, nblk, k, s->part, s->nact, s->ptw);
+        GB_LAUNCH(ctx, k_sum_active, (k + 127) / 128, 128, 0, nblk, k, s->part, s->nact, s->ptw, s->rho2, s->alpha);
         GB_PROF(ctx, GB_K_BCGVEC, 6.0 * es * n * k, 6.0 * n * k);
-        GB_LAUNCH(ctx, k_xr_update<T>, rgrid, 256, 0, n, k, X, R, P, W, ld, s->rho2, s->ptw, s->nact, s->part);
-        GB_LAUNCH(ctx, k_finalize, 1, 256, 0, nblk, k, s->part, s->rho1, s->rho2, s->err, s->nact, a->rate);
+        GB_LAUNCH(ctx, k_xr_update<T>, rgrid, 256, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part);
+        GB_LAUNCH(ctx, k_finalize, 1, 256, 0, nblk, k, s->part, s->rho1, s->rho2, s->err, s->nact, a->rate, s->beta);
     }
     return GCGE_GPU_OK;
 }
@@ -258,6 +264,8 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     s.rho2 = (double *)take(sizeof(double) * k);
     s.err = (double *)take(sizeof(double) * k);
     s.ptw = (double *)take(sizeof(double) * k);
+    s.alpha = (double *)take(sizeof(double) * k);
+    s.beta = (double *)take(sizeof(double) * k);
     s.part = (double *)take(sizeof(double) * (size_t)nblk * k);
     s.nact = (int *)take(64);
     dim3 rgrid(nblk, (k + 31) / 32);
@@ -303,23 +311,20 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     GB_LAUNCH(ctx, k_dot_partial<float>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
     GB_LAUNCH(ctx, k_init_state, 1, 256, 0, nblk, k, s.part, s.rho2, s.err, s.nact);
     if ((st = bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s))) return st;
-    GB_LAUNCH(ctx, k_add_f2d, elem_grid(ctx, (long)n * k), 256, 0, n, k, D, ld, X, ldx);
+    GB_LAUNCH(ctx, k_add_f2d, row_grid(ctx, n), 256, 0, n, k, D, ld, X, ldx);
     return gb_convert_f2d(ctx, n, k, R, ld, RHS, ldr);
 }
 
 __global__ void k_axpy32(int n, int k, float a, const float *__restrict__ X, float *__restrict__ Y, long ld)
 {
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
-        Y[r * ld + c] += a * X[r * ld + c];
-    }
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) Y[r * ld + c] += a * X[r * ld + c];
 }
 
 extern "C" int gb_axpy32(gcge_gpu_ctx *ctx, int n, int k, float a, const float *X, float *Y, long ld)
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
-    GB_LAUNCH(ctx, k_axpy32, elem_grid(ctx, (long)n * k), 256, 0, n, k, a, X, Y, ld);
+    GB_LAUNCH(ctx, k_axpy32, row_grid(ctx, n), 256, 0, n, k, a, X, Y, ld);
     return GCGE_GPU_OK;
 }

@@ -142,18 +142,31 @@ extern "C" int gb_spmm32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const float *
 }
 
 // ---------------------------------------------------------------- AXPBY
+// warp-per-row loop over an n x k block: lanes walk the columns of one row
+#define ROWS_BY_WARP(n, r)                                                             \
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < (n);         \
+         r += ((long)gridDim.x * blockDim.x) >> 5)
+
 __global__ void k_axpby(int n, int k, double a, const double *__restrict__ X, long ldx, double b,
                         double *__restrict__ Y, long ldy)
 {
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) {
         double *y = Y + r * ldy + c;
         if (a == 0.0) *y = b * *y;
         else if (b == 0.0) *y = (a == 1.0) ? X[r * ldx + c] : a * X[r * ldx + c];
         else *y = a * X[r * ldx + c] + b * *y;
     }
+}
+
+// blocks of 8 warps for a warp-per-row loop, capped at 16 blocks per SM
+static int row_grid(gcge_gpu_ctx *ctx, long rows)
+{
+    long g = (rows + 7) / 8, cap = (long)ctx->num_sms * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
 }
 
 static int elem_grid(gcge_gpu_ctx *ctx, long total)
@@ -170,17 +183,16 @@ extern "C" int gb_axpby(gcge_gpu_ctx *ctx, int n, int k, double a, const double 
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
     GB_PROF(ctx, GB_K_BLAS1, (a == 0.0 || b == 0.0 ? 16.0 : 24.0) * n * k, 2.0 * n * k);
-    GB_LAUNCH(ctx, k_axpby, elem_grid(ctx, (long)n * k), 256, 0, n, k, a, X, ldx, b, Y, ldy);
+    GB_LAUNCH(ctx, k_axpby, row_grid(ctx, n), 256, 0, n, k, a, X, ldx, b, Y, ldy);
     return GCGE_GPU_OK;
 }
 
 __global__ void k_gather_cols(int n, int k, const double *__restrict__ X, long ldx, const int *__restrict__ idx,
                               double *__restrict__ Y, long ldy, const double *__restrict__ eval, int mode)
 {
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) {
         const int src = idx ? idx[c] : c;
         double s = 1.0;
         if (mode == 1) {
@@ -196,7 +208,7 @@ extern "C" int gb_gather_cols(gcge_gpu_ctx *ctx, int n, int k, const double *X, 
                               double *Y, long ldy, const double *eval_dev, int mode)
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
-    GB_LAUNCH(ctx, k_gather_cols, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, idx_dev, Y, ldy,
+    GB_LAUNCH(ctx, k_gather_cols, row_grid(ctx, n), 256, 0, n, k, X, ldx, idx_dev, Y, ldy,
               eval_dev, mode);
     return GCGE_GPU_OK;
 }
@@ -226,32 +238,26 @@ extern "C" int gb_fill_random(gcge_gpu_ctx *ctx, int n, int k, double *X, long l
 
 __global__ void k_d2f(int n, int k, const double *__restrict__ X, long ldx, float *__restrict__ Y, long ldy)
 {
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
-        Y[r * ldy + c] = (float)X[r * ldx + c];
-    }
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) Y[r * ldy + c] = (float)X[r * ldx + c];
 }
 __global__ void k_f2d(int n, int k, const float *__restrict__ X, long ldx, double *__restrict__ Y, long ldy)
 {
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
-        Y[r * ldy + c] = (double)X[r * ldx + c];
-    }
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) Y[r * ldy + c] = (double)X[r * ldx + c];
 }
 extern "C" int gb_convert_d2f(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, float *Y, long ldy)
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
-    GB_LAUNCH(ctx, k_d2f, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, Y, ldy);
+    GB_LAUNCH(ctx, k_d2f, row_grid(ctx, n), 256, 0, n, k, X, ldx, Y, ldy);
     return GCGE_GPU_OK;
 }
 extern "C" int gb_convert_f2d(gcge_gpu_ctx *ctx, int n, int k, const float *X, long ldx, double *Y, long ldy)
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
-    GB_LAUNCH(ctx, k_f2d, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, Y, ldy);
+    GB_LAUNCH(ctx, k_f2d, row_grid(ctx, n), 256, 0, n, k, X, ldx, Y, ldy);
     return GCGE_GPU_OK;
 }
 
@@ -551,18 +557,15 @@ extern "C" int gb_select(gcge_gpu_ctx *ctx, int k, const double *src, const int 
 __global__ void k_scale_cols(int n, int k, const double *__restrict__ X, long ldx, const double *__restrict__ s,
                              double *Y, long ldy)
 {
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
-        Y[r * ldy + c] = s[c] * X[r * ldx + c];
-    }
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) Y[r * ldy + c] = s[c] * X[r * ldx + c];
 }
 extern "C" int gb_scale_cols(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, const double *s, double *Y,
                              long ldy)
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
-    GB_LAUNCH(ctx, k_scale_cols, elem_grid(ctx, (long)n * k), 256, 0, n, k, X, ldx, s, Y, ldy);
+    GB_LAUNCH(ctx, k_scale_cols, row_grid(ctx, n), 256, 0, n, k, X, ldx, s, Y, ldy);
     return GCGE_GPU_OK;
 }
 
