@@ -62,6 +62,27 @@ static int grow(gcge_gpu_ctx *ctx, double **p, size_t *cap, size_t n, int pinned
 extern "C" int gb_scratch(gcge_gpu_ctx *ctx, size_t n) { return grow(ctx, &ctx->scratch, &ctx->scratch_cap, n, 0); }
 extern "C" int gb_coef(gcge_gpu_ctx *ctx, size_t n) { return grow(ctx, &ctx->coef, &ctx->coef_cap, n, 0); }
 extern "C" int gb_pinned(gcge_gpu_ctx *ctx, size_t n) { return grow(ctx, &ctx->pinned, &ctx->pinned_cap, n, 1); }
+extern "C" int gb_iscratch(gcge_gpu_ctx *ctx, size_t n)
+{
+    if (ctx->iscratch_cap >= n) return GCGE_GPU_OK;
+    if (ctx->iscratch) {
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+        cudaFree(ctx->iscratch);
+        ctx->iscratch = nullptr;
+        ctx->iscratch_cap = 0;
+    }
+    const size_t want = n + 1024;
+    if (cudaMalloc(&ctx->iscratch, want * sizeof(int)) != cudaSuccess) return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
+    ctx->iscratch_cap = want;
+    return GCGE_GPU_OK;
+}
+
+extern "C" int GCGE_GPU_SetTensorEmulation(gcge_gpu_ctx *ctx, int on)
+{
+    if (!ctx) return GCGE_GPU_ERR_ARG;
+    ctx->tc = on ? 1 : 0;
+    return GCGE_GPU_OK;
+}
 
 // ---------------------------------------------------------------- context
 extern "C" int GCGE_GPU_Init(int device, gcge_gpu_ctx **out)
@@ -80,7 +101,9 @@ extern "C" int GCGE_GPU_Init(int device, gcge_gpu_ctx **out)
         free(c);
         return GCGE_GPU_ERR_CUDA;
     }
+    c->tc = 1;
     int st = gb_scratch(c, 1 << 20);
+    if (!st) st = gb_iscratch(c, 4096);
     if (!st) st = gb_coef(c, 1 << 16);
     if (!st) st = gb_pinned(c, 1 << 16);
     if (st) {
@@ -104,6 +127,7 @@ extern "C" int GCGE_GPU_Finalize(gcge_gpu_ctx *ctx)
         free(ctx->prof_flops);
     }
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->iscratch) cudaFree(ctx->iscratch);
     if (ctx->coef) cudaFree(ctx->coef);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     cudaStreamDestroy(ctx->stream);

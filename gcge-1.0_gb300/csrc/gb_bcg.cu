@@ -21,7 +21,7 @@
 
 #include "gb_internal.h"
 
-#define RED_ROWS 1024
+#define RED_ROWS 128
 
 extern "C" int gb_axpy32(gcge_gpu_ctx *ctx, int n, int k, float a, const float *X, float *Y, long ld);
 
@@ -40,7 +40,7 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
     } while (0)
 
 struct bcg_state {
-    double *rho1, *rho2, *err, *ptw, *part, *alpha, *beta;
+    double *rho1, *rho2, *err, *ptw, *part, *alpha, *beta, *sums;
     int *nact;
 };
 
@@ -138,33 +138,46 @@ k_xr_update(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restr
     }
 }
 
-// ptw[c] = sum of partials for active c, and alpha[c] = rho2[c] / ptw[c]
-__global__ void k_sum_active(int nblk, int k, const double *__restrict__ part, const int *__restrict__ nact,
-                             double *__restrict__ out, const double *__restrict__ rho2, double *__restrict__ alpha)
+// second stage of the per-column sums, one block per column: each thread adds a
+// fixed strided subset of the row-slab partials, then a fixed tree (deterministic)
+__global__ void __launch_bounds__(256)
+k_colsum(int nblk, int k, const double *__restrict__ part, const int *__restrict__ nact, double *__restrict__ out)
+{
+    __shared__ double sh[256];
+    const int c = blockIdx.x;
+    if (nact && c >= *nact) return;
+    double s = 0;
+    for (int b = threadIdx.x; b < nblk; b += 256) s += part[(long)b * k + c];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = sh[0];
+}
+
+// ptw[c] (summed by k_colsum) for active c, and alpha[c] = rho2[c] / ptw[c]
+__global__ void k_sum_active(int k, const int *__restrict__ nact, const double *__restrict__ ptw,
+                             const double *__restrict__ rho2, double *__restrict__ alpha)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k || c >= *nact) return;
-    double s = 0;
-    for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
-    out[c] = s;
-    alpha[c] = rho2[c] / s;
+    alpha[c] = rho2[c] / ptw[c];
 }
 
-// initial residual norms: rho2 = sum partials, err = sqrt(rho2), nact = k
-__global__ void k_init_state(int nblk, int k, const double *__restrict__ part, double *rho2, double *err,
-                             int *nact)
+// initial residual norms: rho2 = column sums, err = sqrt(rho2), nact = k
+__global__ void k_init_state(int k, const double *__restrict__ sums, double *rho2, double *err, int *nact)
 {
     for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        double s = 0;
-        for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
-        rho2[c] = s;
-        err[c] = sqrt(s);
+        rho2[c] = sums[c];
+        err[c] = sqrt(sums[c]);
     }
     if (threadIdx.x == 0) *nact = k;
 }
 
 // end of a round: rho1 = rho2, rho2 = new r.r (active columns); recount over all columns
-__global__ void k_finalize(int nblk, int k, const double *__restrict__ part, double *rho1, double *rho2,
+__global__ void k_finalize(int k, const double *__restrict__ sums, double *rho1, double *rho2,
                            const double *__restrict__ err, int *nact, double rate, double *beta)
 {
     __shared__ int cnt;
@@ -173,8 +186,7 @@ __global__ void k_finalize(int nblk, int k, const double *__restrict__ part, dou
     __syncthreads();
     for (int c = threadIdx.x; c < k; c += blockDim.x) {
         if (c < ka) {
-            double s = 0;
-            for (int b = 0; b < nblk; ++b) s += part[(long)b * k + c];
+            const double s = sums[c];
             rho1[c] = rho2[c];
             rho2[c] = s;
             beta[c] = s / rho1[c];   // the next round's beta (src/gcge_cg.c:645)
@@ -213,11 +225,11 @@ static int elem_grid(gcge_gpu_ctx *ctx, long total)
 
 extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
 {
-    long ldk = (k + 1) & ~1;
+    long ldk = (k + 3) & ~3;   // 16-byte rows for the vectorised SpMM
     size_t vec = precision ? sizeof(float) : sizeof(double);
     size_t nblk = (size_t)cdiv(n > 0 ? n : 1, RED_ROWS);
     size_t blocks = 4 * (size_t)n * ldk * vec;  // R, X, P, W
-    size_t state = (6 * (size_t)k + nblk * (size_t)k + 8) * sizeof(double) + 64;
+    size_t state = (7 * (size_t)k + nblk * (size_t)k + 8) * sizeof(double) + 64;
     return blocks + state + 16 * 256;   // every sub-buffer is aligned to 256 bytes (10 of them)
 }
 
@@ -239,10 +251,12 @@ static int bcg_rounds(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, T *R, T *X, T *P
         if (st) return st;
         GB_PROF(ctx, GB_K_BCGVEC, 2.0 * es * n * k, 2.0 * n * k);
         GB_LAUNCH(ctx, k_dot_partial<T>, rgrid, 256, 0, n, k, P, W, ld, s->nact, s->part);
-        GB_LAUNCH(ctx, k_sum_active, (k + 127) / 128, 128, 0, nblk, k, s->part, s->nact, s->ptw, s->rho2, s->alpha);
+        GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s->part, s->nact, s->ptw);
+        GB_LAUNCH(ctx, k_sum_active, (k + 127) / 128, 128, 0, k, s->nact, s->ptw, s->rho2, s->alpha);
         GB_PROF(ctx, GB_K_BCGVEC, 6.0 * es * n * k, 6.0 * n * k);
         GB_LAUNCH(ctx, k_xr_update<T>, rgrid, 256, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part);
-        GB_LAUNCH(ctx, k_finalize, 1, 256, 0, nblk, k, s->part, s->rho1, s->rho2, s->err, s->nact, a->rate, s->beta);
+        GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s->part, s->nact, s->sums);
+        GB_LAUNCH(ctx, k_finalize, 1, 256, 0, k, s->sums, s->rho1, s->rho2, s->err, s->nact, a->rate, s->beta);
     }
     return GCGE_GPU_OK;
 }
@@ -254,7 +268,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     if (k <= 0 || n <= 0) return GCGE_GPU_OK;
     if (work_bytes < gb_bcg_work_bytes(n, k, a->precision)) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     if (a->precision && !A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
-    const long ld = (k + 1) & ~1;
+    const long ld = (k + 3) & ~3;
     const int nblk = cdiv(n, RED_ROWS);
     char *w = (char *)work;
     size_t vec = a->precision ? sizeof(float) : sizeof(double);
@@ -266,6 +280,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     s.ptw = (double *)take(sizeof(double) * k);
     s.alpha = (double *)take(sizeof(double) * k);
     s.beta = (double *)take(sizeof(double) * k);
+    s.sums = (double *)take(sizeof(double) * k);
     s.part = (double *)take(sizeof(double) * (size_t)nblk * k);
     s.nact = (int *)take(64);
     dim3 rgrid(nblk, (k + 31) / 32);
@@ -279,7 +294,8 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
         // P and W use the compact ld; R and X keep their own ld through the copies below
         if (ldr == ld && ldx == ld) {
             GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, RHS, RHS, ld, (const int *)nullptr, s.part);
-            GB_LAUNCH(ctx, k_init_state, 1, 256, 0, nblk, k, s.part, s.rho2, s.err, s.nact);
+            GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
+            GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
             return bcg_rounds<double>(ctx, A, RHS, X, P, W, ld, a, &s);
         }
         // general leading dimensions: stage R and X in compact blocks
@@ -289,7 +305,8 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
         if ((st = gb_axpby(ctx, n, k, 1.0, RHS, ldr, 0.0, R, ld))) return st;
         if ((st = gb_axpby(ctx, n, k, 1.0, X, ldx, 0.0, Xc, ld))) return st;
         GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
-        GB_LAUNCH(ctx, k_init_state, 1, 256, 0, nblk, k, s.part, s.rho2, s.err, s.nact);
+        GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
+            GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
         if ((st = bcg_rounds<double>(ctx, A, R, Xc, P, W, ld, a, &s))) return st;
         if ((st = gb_axpby(ctx, n, k, 1.0, Xc, ld, 0.0, X, ldx))) return st;
         return gb_axpby(ctx, n, k, 1.0, R, ld, 0.0, RHS, ldr);
@@ -309,7 +326,8 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     if (cudaMemsetAsync(D, 0, (size_t)n * ld * sizeof(float), ctx->stream) != cudaSuccess)
         return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
     GB_LAUNCH(ctx, k_dot_partial<float>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
-    GB_LAUNCH(ctx, k_init_state, 1, 256, 0, nblk, k, s.part, s.rho2, s.err, s.nact);
+    GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
+    GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
     if ((st = bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s))) return st;
     GB_LAUNCH(ctx, k_add_f2d, row_grid(ctx, n), 256, 0, n, k, D, ld, X, ldx);
     return gb_convert_f2d(ctx, n, k, R, ld, RHS, ldr);

@@ -79,6 +79,85 @@ k_spmm(int n, const int *__restrict__ rp, const int *__restrict__ ci, const VT *
     }
 }
 
+// Vectorised SpMM: a group of L lanes (L = 8, 16 or 32) owns one row and VW =
+// 16 / sizeof(T) consecutive columns per lane, so each nonzero gathers its block
+// row of X with one 16-byte load per lane; 32 / L rows per warp. The group loads
+// up to L (column, value) pairs at once and broadcasts them with group-masked
+// shuffles. Needs X, Y and their leading dimensions 16-byte aligned.
+template <typename T> struct vec16;
+template <> struct vec16<float> { typedef float4 type; };
+template <> struct vec16<double> { typedef double2 type; };
+
+template <typename T, int L>
+__global__ void __launch_bounds__(256)
+k_spmm_vec(int n, const int *__restrict__ rp, const int *__restrict__ ci, const T *__restrict__ val,
+           const T *__restrict__ X, long ldx, T *__restrict__ Y, long ldy, int k, T alpha,
+           const double *__restrict__ alpha_col, T beta, const int *__restrict__ ncols_dev)
+{
+    typedef typename vec16<T>::type V;
+    constexpr int VW = 16 / sizeof(T);
+    constexpr int RPW = 32 / L;
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / L, sl = lane % L;
+    const unsigned gmask = (L == 32) ? FULL : (((1u << L) - 1u) << (sub * L));
+    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long row = warp * RPW + sub;
+    int kact = k;
+    if (ncols_dev) kact = min(k, *ncols_dev);
+    if (row >= n || kact <= 0) return;                    // uniform within the row group
+    const int beg = rp[row], end = rp[row + 1];
+    for (int c0 = 0; c0 < kact; c0 += L * VW) {
+        const int c = c0 + sl * VW;
+        const bool full = c + VW <= kact;
+        T acc[VW];
+#pragma unroll
+        for (int q = 0; q < VW; ++q) acc[q] = 0;
+        for (int base = beg; base < end; base += L) {
+            const int e = base + sl;
+            int j = 0;
+            T a = 0;
+            if (e < end) { j = __ldg(ci + e); a = __ldg(val + e); }
+            const int cnt = min(L, end - base);
+#pragma unroll 4
+            for (int t = 0; t < cnt; ++t) {
+                const int jj = __shfl_sync(gmask, j, t, L);
+                const T aa = __shfl_sync(gmask, a, t, L);
+                const T *xr = X + (long)jj * ldx + c;
+                if (full) {
+                    const V xv = __ldg(reinterpret_cast<const V *>(xr));
+                    const T *xs = reinterpret_cast<const T *>(&xv);
+#pragma unroll
+                    for (int q = 0; q < VW; ++q) acc[q] = fma(aa, xs[q], acc[q]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < VW; ++q)
+                        if (c + q < kact) acc[q] = fma(aa, __ldg(xr + q), acc[q]);
+                }
+            }
+        }
+        T *yr = Y + row * ldy + c;
+#pragma unroll
+        for (int q = 0; q < VW; ++q) {
+            if (c + q >= kact) break;
+            const T s = alpha * (alpha_col ? (T)alpha_col[c + q] : (T)1);
+            yr[q] = beta == (T)0 ? s * acc[q] : s * acc[q] + beta * yr[q];
+        }
+    }
+}
+
+// lanes per row for the vectorised SpMM: the smallest of 8/16/32 covering k
+template <typename T>
+static int spmm_vec_lanes(int k)
+{
+    const int need = (k + (16 / (int)sizeof(T)) - 1) / (16 / (int)sizeof(T));
+    return need <= 8 ? 8 : (need <= 16 ? 16 : 32);
+}
+
+static bool aligned16(const void *p, long ld, size_t es)
+{
+    return ((uintptr_t)p & 15u) == 0 && ((ld * (long)es) & 15) == 0;
+}
+
 // single-column SpMV: a warp splits the row's nonzeros, shuffle reduction
 template <typename VT, typename XT, typename AT>
 __global__ void __launch_bounds__(256)
@@ -113,10 +192,25 @@ extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X
         GB_LAUNCH(ctx, (k_spmv<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
                   Y, ldy, alpha, alpha_col, beta, ncols_dev);
     } else {
-        long warps = (long)A->n * ((k + 63) / 64);
-        int grid = ceil_div_l(warps * 32, 256);
-        GB_LAUNCH(ctx, (k_spmm<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
-                  Y, ldy, k, alpha, alpha_col, beta, ncols_dev);
+        if (aligned16(X, ldx, sizeof(double)) && aligned16(Y, ldy, sizeof(double))) {
+            const int L = spmm_vec_lanes<double>(k);
+            const long warps = ((long)A->n * L + 31) / 32;
+            const int grid = ceil_div_l(warps * 32, 256);
+            if (L == 8)
+                GB_LAUNCH(ctx, (k_spmm_vec<double, 8>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
+                          alpha, alpha_col, beta, ncols_dev);
+            else if (L == 16)
+                GB_LAUNCH(ctx, (k_spmm_vec<double, 16>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
+                          alpha, alpha_col, beta, ncols_dev);
+            else
+                GB_LAUNCH(ctx, (k_spmm_vec<double, 32>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
+                          alpha, alpha_col, beta, ncols_dev);
+        } else {
+            long warps = (long)A->n * ((k + 63) / 64);
+            int grid = ceil_div_l(warps * 32, 256);
+            GB_LAUNCH(ctx, (k_spmm<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
+                      Y, ldy, k, alpha, alpha_col, beta, ncols_dev);
+        }
     }
     return GCGE_GPU_OK;
 }
@@ -133,10 +227,25 @@ extern "C" int gb_spmm32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const float *
         GB_LAUNCH(ctx, (k_spmv<float, float, float>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx,
                   Y, ldy, 1.0f, (const double *)nullptr, 0.0f, ncols_dev);
     } else {
-        long warps = (long)A->n * ((k + 63) / 64);
-        int grid = ceil_div_l(warps * 32, 256);
-        GB_LAUNCH(ctx, (k_spmm<float, float, float>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y,
-                  ldy, k, 1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+        if (aligned16(X, ldx, sizeof(float)) && aligned16(Y, ldy, sizeof(float))) {
+            const int L = spmm_vec_lanes<float>(k);
+            const long warps = ((long)A->n * L + 31) / 32;
+            const int grid = ceil_div_l(warps * 32, 256);
+            if (L == 8)
+                GB_LAUNCH(ctx, (k_spmm_vec<float, 8>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y, ldy, k,
+                          1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+            else if (L == 16)
+                GB_LAUNCH(ctx, (k_spmm_vec<float, 16>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y, ldy, k,
+                          1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+            else
+                GB_LAUNCH(ctx, (k_spmm_vec<float, 32>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y, ldy, k,
+                          1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+        } else {
+            long warps = (long)A->n * ((k + 63) / 64);
+            int grid = ceil_div_l(warps * 32, 256);
+            GB_LAUNCH(ctx, (k_spmm<float, float, float>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y,
+                      ldy, k, 1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+        }
     }
     return GCGE_GPU_OK;
 }
@@ -434,6 +543,11 @@ extern "C" int gb_gram(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *V
                        long ldw, double *a_dev, int lda, int sym)
 {
     if (k1 <= 0 || k2 <= 0) return GCGE_GPU_OK;
+    if (ctx->tc) {
+        int st = gb_iscratch(ctx, (size_t)k1 + k2);
+        if (st) return st;
+        return gb_gram_tc(ctx, n, k1, k2, V, ldv, W, ldw, a_dev, lda, sym, ctx->iscratch);
+    }
     const int ti = (k1 + 31) / 32, tj = (k2 + 31) / 32;
     int tiles = sym ? ti * (ti + 1) / 2 : ti * tj;
     if (tiles < 1) tiles = 1;
@@ -597,5 +711,13 @@ extern "C" int gb_gram_fixed_scratch(cudaStream_t stream, int num_sms, int n, in
     if (g > (long)num_sms * 16) g = (long)num_sms * 16;
     k_gram_reduce<<<(int)(g > 0 ? g : 1), 256, 0, stream>>>(k1, k2, (int)nsplit, part, a_dev, lda, sym);
     if (cudaGetLastError() != cudaSuccess) return GCGE_GPU_ERR_CUDA;
+    return GCGE_GPU_OK;
+}
+
+// second stage of a Gram product whose per-split partials are already in part
+extern "C" int gb_gram_reduce_launch(gcge_gpu_ctx *ctx, int k1, int k2, int nsplit, const double *part,
+                                     double *a_dev, int lda, int sym)
+{
+    GB_LAUNCH(ctx, k_gram_reduce, elem_grid(ctx, (long)k1 * k2), 256, 0, k1, k2, nsplit, part, a_dev, lda, sym);
     return GCGE_GPU_OK;
 }

@@ -47,6 +47,11 @@ struct gcge_gpu_ctx {
     double *prof_bytes, *prof_flops;
     double cls_ms[GB_PROF_CLASSES], cls_bytes[GB_PROF_CLASSES], cls_flops[GB_PROF_CLASSES];
     long long cls_launches[GB_PROF_CLASSES];
+    /* dense FP64 contractions (Gram, linear combination) on the bf16 tensor cores
+     * with an error-free digit splitting (1, default) or on the FP64 pipe (0) */
+    int tc;
+    int *iscratch;
+    size_t iscratch_cap;
 };
 
 struct gcge_gpu_mat {
@@ -76,6 +81,10 @@ int gb_check_launch(gcge_gpu_ctx *ctx);
 int gb_scratch(gcge_gpu_ctx *ctx, size_t n);
 int gb_coef(gcge_gpu_ctx *ctx, size_t n);
 int gb_pinned(gcge_gpu_ctx *ctx, size_t n);
+int gb_iscratch(gcge_gpu_ctx *ctx, size_t n);
+/* FP64-accurate Gram on the tensor cores (gb_ozaki.cu); exps: int[k1 + k2] */
+int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *V, long ldv, const double *W, long ldw,
+               double *a_dev, int lda, int sym, int *exps);
 
 /* ------------------------------------------------------------ gb_blas.cu */
 /* Y[:, 0:k] = alpha_c * (A X[:, 0:k]) + beta * Y, alpha_c = alpha * (alpha_col ? alpha_col[c] : 1).

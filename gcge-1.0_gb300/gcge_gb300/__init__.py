@@ -96,6 +96,7 @@ def load():
         "GCGE_GPU_OpsMultiVecBlock": (_I, [_P, C.POINTER(_P), C.POINTER(_I)]),
         "GCGE_GPU_ProfileEnable": (_I, [_P, _I]),
         "GCGE_GPU_ProfileRead": (_I, [_P, _I, _P, _P, _P, _P, _I]),
+        "GCGE_GPU_SetTensorEmulation": (_I, [_P, _I]),
         "GCGE_GPU_InnerProdNoAlloc": (_I, [_I, _I, _I, _P, C.c_long, _P, C.c_long, _P, _I, _I, _P]),
     }
     for name, (res, args) in sig.items():
@@ -171,6 +172,10 @@ class Context:
 
     def sync(self):
         _chk(self.lib.GCGE_GPU_Synchronize(self.h), "sync")
+
+    def tensor_emulation(self, on):
+        """Dense FP64 contractions on the tensor cores (error-free splitting) or the FP64 pipe."""
+        _chk(self.lib.GCGE_GPU_SetTensorEmulation(self.h, int(on)), "SetTensorEmulation")
 
     def last_error(self):
         return self.lib.GCGE_GPU_GetLastError(self.h)

@@ -85,6 +85,12 @@ int  GCGE_GPU_MultiVecDownload(const gcge_gpu_mv *mv, int col0, int ncols, doubl
  * (seed, column*n + row); ops->MultiVecSetRandomValue, src/gcge_ops.h:66. */
 int  GCGE_GPU_MultiVecSetRandomValue(gcge_gpu_mv *mv, int start, int nvec, unsigned long long seed);
 
+/* Dense FP64 contractions (Gram products, linear combinations) either on the
+ * bf16 tensor cores with an error-free digit splitting that keeps FP64 accuracy
+ * (on = 1, the default) or on the FP64 pipe (on = 0). No counterpart in the
+ * reference (its dense work is host BLAS). */
+int  GCGE_GPU_SetTensorEmulation(gcge_gpu_ctx *ctx, int on);
+
 /* ---- 2. block operations (semantics of src/gcge_ops.c:115-300) ---- */
 
 /* y(:, start[1]:end[1]) = A x(:, start[0]:end[0]); ops->MatDotMultiVec,
