@@ -77,6 +77,35 @@ extern "C" int gb_iscratch(gcge_gpu_ctx *ctx, size_t n)
     return GCGE_GPU_OK;
 }
 
+// after a stream synchronisation: GCGE_GPU_ERR_TIMEOUT when a kernel reported
+// that one of its bounded waits ran out (its results are then invalid)
+extern "C" int gb_check_device_error(gcge_gpu_ctx *ctx)
+{
+    int h = 0;
+    if (cudaMemcpyAsync(&h, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+    return h ? gb_fail(ctx, GCGE_GPU_ERR_TIMEOUT) : GCGE_GPU_OK;
+}
+
+extern "C" int gb_ozbuf(gcge_gpu_ctx *ctx, size_t bytes)
+{
+    if (ctx->ozbuf_cap >= bytes) return GCGE_GPU_OK;
+    if (ctx->ozbuf) {
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+        cudaFree(ctx->ozbuf);
+        ctx->ozbuf = nullptr;
+        ctx->ozbuf_cap = 0;
+    }
+    const size_t want = bytes + bytes / 4 + 4096;
+    if (cudaMalloc(&ctx->ozbuf, want) != cudaSuccess) {
+        ctx->ozbuf = nullptr;
+        return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
+    }
+    ctx->ozbuf_cap = want;
+    return GCGE_GPU_OK;
+}
+
 extern "C" int GCGE_GPU_SetTensorEmulation(gcge_gpu_ctx *ctx, int on)
 {
     if (!ctx) return GCGE_GPU_ERR_ARG;
@@ -106,6 +135,10 @@ extern "C" int GCGE_GPU_Init(int device, gcge_gpu_ctx **out)
     if (!st) st = gb_iscratch(c, 4096);
     if (!st) st = gb_coef(c, 1 << 16);
     if (!st) st = gb_pinned(c, 1 << 16);
+    if (!st) st = gb_ozbuf(c, 1 << 20);
+    if (!st && (cudaMalloc(&c->dev_err, sizeof(int)) != cudaSuccess ||
+                cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream) != cudaSuccess))
+        st = GCGE_GPU_ERR_NOMEM;
     if (st) {
         GCGE_GPU_Finalize(c);
         return st;
@@ -130,6 +163,8 @@ extern "C" int GCGE_GPU_Finalize(gcge_gpu_ctx *ctx)
     if (ctx->iscratch) cudaFree(ctx->iscratch);
     if (ctx->coef) cudaFree(ctx->coef);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->ozbuf) cudaFree(ctx->ozbuf);
+    if (ctx->dev_err) cudaFree(ctx->dev_err);
     cudaStreamDestroy(ctx->stream);
     free(ctx);
     return GCGE_GPU_OK;
@@ -154,6 +189,7 @@ extern "C" const char *GCGE_GPU_ErrorString(int st)
     case GCGE_GPU_ERR_NONFINITE: return "non-finite value";
     case GCGE_GPU_ERR_BREAKDOWN: return "orthogonalisation lost every column";
     case GCGE_GPU_ERR_EIGSOLVE: return "projected eigensolve failed";
+    case GCGE_GPU_ERR_TIMEOUT: return "tensor-core kernel wait timed out";
     default: return "unknown status";
     }
 }
@@ -162,7 +198,7 @@ extern "C" int GCGE_GPU_Synchronize(gcge_gpu_ctx *ctx)
 {
     if (!ctx) return GCGE_GPU_ERR_ARG;
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    return GCGE_GPU_OK;
+    return gb_check_device_error(ctx);
 }
 
 extern "C" long long GCGE_GPU_LaunchCount(const gcge_gpu_ctx *ctx) { return ctx ? ctx->launches : 0; }

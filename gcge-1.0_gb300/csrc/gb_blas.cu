@@ -624,6 +624,7 @@ extern "C" int gb_lincomb(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double
 {
     if (n <= 0 || k2 <= 0) return GCGE_GPU_OK;
     if (k1 <= 0) return gb_axpby(ctx, n, k2, 0.0, Y, ldy, beta, Y, ldy);
+    if (ctx->tc && gb_lincomb_tc_ok(k1)) return gb_lincomb_tc(ctx, n, k1, k2, X, ldx, C_dev, ldc, alpha, beta, Y, ldy, upper);
     dim3 grid(ceil_div_l(n, 64), (k2 + 31) / 32);
     GB_PROF(ctx, GB_K_LINCOMB, 8.0 * n * k1 + (beta != 0.0 ? 16.0 : 8.0) * n * k2,
             upper ? 1.0 * n * k1 * (k2 + 1) : 2.0 * n * k1 * k2);

@@ -52,6 +52,9 @@ struct gcge_gpu_ctx {
     int tc;
     int *iscratch;
     size_t iscratch_cap;
+    void *ozbuf;               /* pre-split digit planes of small operands */
+    size_t ozbuf_cap;          /* bytes */
+    int *dev_err;              /* device word: set by a kernel whose bounded wait ran out */
 };
 
 struct gcge_gpu_mat {
@@ -82,9 +85,16 @@ int gb_scratch(gcge_gpu_ctx *ctx, size_t n);
 int gb_coef(gcge_gpu_ctx *ctx, size_t n);
 int gb_pinned(gcge_gpu_ctx *ctx, size_t n);
 int gb_iscratch(gcge_gpu_ctx *ctx, size_t n);
+int gb_ozbuf(gcge_gpu_ctx *ctx, size_t bytes);
+int gb_check_device_error(gcge_gpu_ctx *ctx);
 /* FP64-accurate Gram on the tensor cores (gb_ozaki.cu); exps: int[k1 + k2] */
 int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *V, long ldv, const double *W, long ldw,
                double *a_dev, int lda, int sym, int *exps);
+/* FP64-accurate Y = alpha X C + beta Y on the tensor cores (gb_ozaki.cu), for k1 where
+ * gb_lincomb_tc_ok(k1) holds */
+int gb_lincomb_tc_ok(int k1);
+int gb_lincomb_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *X, long ldx, const double *C, int ldc,
+                  double alpha, double beta, double *Y, long ldy, int upper);
 
 /* ------------------------------------------------------------ gb_blas.cu */
 /* Y[:, 0:k] = alpha_c * (A X[:, 0:k]) + beta * Y, alpha_c = alpha * (alpha_col ? alpha_col[c] : 1).

@@ -567,6 +567,7 @@ int GCGE_GPU_Solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat 
 
     CTRY(cudaEventRecord(e1, ctx->stream));
     CTRY(cudaStreamSynchronize(ctx->stream));
+    TRY(gb_check_device_error(ctx));
     ph_collect(g);
     memcpy(eval, g->eval_h, sizeof(double) * nev);
     if (stats) {

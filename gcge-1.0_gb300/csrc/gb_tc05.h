@@ -1,0 +1,210 @@
+// gb_tc05.h -- inline-PTX primitives for the 5th-generation tensor cores
+// (tcgen05: TMEM accumulators, shared-memory operand descriptors, mbarriers)
+// and the error-free FP64 digit splitting shared by the tensor-core kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+// ---------------------------------------------------------------- addresses, fences
+__device__ __forceinline__ uint32_t tc_smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void tc_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ uint64_t tc_globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---------------------------------------------------------------- TMEM
+// allocation by one whole warp; the TMEM address is written to smem[dst]
+__device__ __forceinline__ void tc_tmem_alloc(uint32_t dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// 32 lanes x 8 consecutive 32-bit columns (lane = warp's quarter of the 128 lanes);
+// the values may be used only after tc_tmem_wait8 on the same registers
+__device__ __forceinline__ void tc_tmem_ld8(uint32_t taddr, uint32_t r[8])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tc_tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// ties registers loaded by tc_tmem_ld8 to a point after tc_tmem_wait_ld
+__device__ __forceinline__ void tc_reg_fence8(uint32_t r[8])
+{
+    asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]));
+}
+
+// ---------------------------------------------------------------- mbarrier
+__device__ __forceinline__ void tc_mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool tc_mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void tc_mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// barrier over the first `count` threads of the CTA (named barrier `id`, 1..15)
+__device__ __forceinline__ void tc_bar_sync(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+// bounded wait for the phase of the given parity; false after limit_ns
+__device__ __forceinline__ bool tc_mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns)
+{
+    if (tc_mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = tc_globaltimer();
+    while (!tc_mbar_try_wait(bar, parity))
+        if (tc_globaltimer() - t0 > limit_ns) return false;
+    return true;
+}
+
+// ---------------------------------------------------------------- MMA
+// shared-memory matrix descriptor, no swizzle: 8-row x 16-byte core matrices of
+// 128 contiguous bytes; lbo = byte distance of core matrices adjacent in K,
+// sbo = byte distance of core matrices adjacent in M (or N)
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+// instruction descriptor of kind::f16: bf16 x bf16 -> f32, both K-major, M x N
+__host__ __device__ constexpr uint32_t tc_idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// the same for f16 x f16 -> f32
+__host__ __device__ constexpr uint32_t tc_idesc_f16(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// D[tmem] (+)= A[smem] * B[smem]^T (kind::f16, types from idesc), issued by one thread
+__device__ __forceinline__ void tc_mma_kf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+// mbarrier arrive once all tcgen05 operations issued so far by this thread are done
+__device__ __forceinline__ void tc_mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// ---------------------------------------------------------------- error-free digit splitting
+// An FP64 entry x of a row (or column) with scale 2^e (|x| < 2^e over the row)
+// is the integer T = x 2^(54 - e), |T| <= 2^54, exact to 2^(e - 54). With the
+// bias B = 0x80808080808080, U = T + B lies in [0, 2^56) and its seven bytes
+// b_0 (least significant) .. b_6 give balanced digits b - 128 in [-128, 127]:
+//   x = sum_p (b_(6-p) - 128) 2^(-8p) 2^(e - 6),   p = 0 (most significant) .. 6.
+// Only integer operations touch x; every digit is exact in f16 (and bf16).
+#define OZ_DIGITS 7
+#define OZ_NO_EXP (-2000)          // scale of an all-zero row or column
+#define OZ_BIAS 0x80808080808080ULL
+
+__device__ __forceinline__ unsigned long long oz_bias(double x, int e)
+{
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    long long T = 0;
+    if (ex) {
+        const long long mant = (b & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+        const int sh = ex - 1021 - e;                    // T = mant 2^sh, sh <= 1
+        if (sh >= 0) T = mant << sh;
+        else if (sh > -60) T = (mant + (1LL << (-sh - 1))) >> (-sh);
+        if (b < 0) T = -T;
+    }
+    return (unsigned long long)T + OZ_BIAS;
+}
+// exponent contribution of one entry: |x| < 2^(ex - 1022); OZ_NO_EXP for 0 and subnormals
+__device__ __forceinline__ int oz_exponent(double x)
+{
+    const int ex = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+    return ex ? ex - 1022 : OZ_NO_EXP;
+}
+// digit p of two biased values as one f16x2 word (u0 in the low half): the
+// bytes b are placed as 0x64bb = 1024 + b and 1152 is subtracted, both exact
+__device__ __forceinline__ uint32_t oz_pack(unsigned long long u0, unsigned long long u1, int p)
+{
+    const int byte = 6 - p, b = byte & 3;
+    const uint32_t w0 = byte < 4 ? (uint32_t)u0 : (uint32_t)(u0 >> 32);
+    const uint32_t w1 = byte < 4 ? (uint32_t)u1 : (uint32_t)(u1 >> 32);
+    const uint32_t t = __byte_perm(w0, w1, (uint32_t)(b | (b << 4) | ((b + 4) << 8) | ((b + 4) << 12)));
+    const uint32_t h = (t & 0x00FF00FFu) | 0x64006400u;
+    uint32_t r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(h), "r"(0x64806480u));
+    return r;
+}
+
+// ---------------------------------------------------------------- exact integer -> FP64
+// (hi 2^32 + lo) 2^(s - 48) rounded once to nearest-even
+__device__ __forceinline__ double oz_to_double(long long hi, long long lo, int s)
+{
+    __int128 z = ((__int128)hi << 32) + (__int128)lo;
+    if (z == 0) return 0.0;
+    unsigned long long sign = 0;
+    if (z < 0) {
+        sign = 1ull << 63;
+        z = -z;
+    }
+    const unsigned __int128 u = (unsigned __int128)z;
+    const unsigned long long zh = (unsigned long long)(u >> 64), zl = (unsigned long long)u;
+    const int nb = zh ? 128 - __clzll((long long)zh) : 64 - __clzll((long long)zl);
+    int E = nb - 1 + s - 48;
+    unsigned long long m;
+    if (nb <= 53) {
+        m = zl << (53 - nb);
+    } else {
+        const int sh = nb - 53;
+        const unsigned __int128 q = u >> sh;
+        const unsigned __int128 rem = u - (q << sh);
+        const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        m = (unsigned long long)q;
+        if (rem > half || (rem == half && (m & 1))) ++m;
+        if (m >> 53) {
+            m >>= 1;
+            ++E;
+        }
+    }
+    if (E < -1022 || E > 1023) {                   // outside the normal range: scale in FP64
+        const double v = ldexp((double)hi, s - 16) + ldexp((double)lo, s - 48);
+        return v;
+    }
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(E + 1023) << 52) |
+                                            (m & ((1ull << 52) - 1))));
+}
+
+// levels 0..6 (exact FP32 integers) -> hi (levels 0-2, units 2^-16) and
+// lo (levels 3-6, units 2^-48) of one output
+__device__ __forceinline__ void oz_levels_to_int(const float v[OZ_DIGITS], long long &hi, long long &lo)
+{
+    hi = ((long long)__float2int_rn(v[0]) << 16) + ((long long)__float2int_rn(v[1]) << 8) +
+         (long long)__float2int_rn(v[2]);
+    lo = ((long long)__float2int_rn(v[3]) << 24) + ((long long)__float2int_rn(v[4]) << 16) +
+         ((long long)__float2int_rn(v[5]) << 8) + (long long)__float2int_rn(v[6]);
+}

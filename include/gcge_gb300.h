@@ -47,6 +47,7 @@ extern "C" {
 #define GCGE_GPU_ERR_NONFINITE 5   /* NaN/Inf met in a reduction or the small eigensolve */
 #define GCGE_GPU_ERR_BREAKDOWN 6   /* orthogonalisation lost every column               */
 #define GCGE_GPU_ERR_EIGSOLVE  7   /* projected eigensolve did not converge             */
+#define GCGE_GPU_ERR_TIMEOUT   8   /* a tensor-core kernel's bounded wait ran out       */
 
 typedef struct gcge_gpu_ctx gcge_gpu_ctx;  /* device, stream, reduction scratch  */
 typedef struct gcge_gpu_mat gcge_gpu_mat;  /* CSR matrix resident in HBM         */

@@ -84,3 +84,100 @@ def test_tensor_gram_symmetric(ctx):
     assert np.array_equal(a, a.T)
     ref = V.T @ V
     assert np.max(np.abs(a - ref)) / np.max(np.abs(ref)) < 1e-14
+
+
+def lincomb(ctx, X, C, tc=True):
+    ctx.tensor_emulation(tc)
+    try:
+        n, k1 = X.shape
+        k2 = C.shape[1]
+        x, y = ctx.multivec(n, k1, X), ctx.multivec(n, k2 + 1, np.full((n, k2 + 1), 3.0))
+        G.multivec_linear_comb(x, y, (0, 1), (k1, 1 + k2), np.asfortranarray(C).ravel(order="F"), k1)
+        out = y.download()
+        assert np.all(out[:, 0] == 3.0)           # the column outside the range is untouched
+        return out[:, 1:]
+    finally:
+        ctx.tensor_emulation(True)
+
+
+@pytest.mark.parametrize("n,k1,k2", [(1000, 37, 21), (100003, 178, 50), (5000, 64, 64), (20000, 100, 130),
+                                     (77, 3, 5), (300, 1, 1), (4099, 129, 17)])
+def test_tensor_lincomb_matches_fp64_pipe(ctx, n, k1, k2):
+    rng = np.random.default_rng(n * 7 + k1)
+    X = rng.standard_normal((n, k1)) * np.exp2(rng.integers(-8, 8, size=(n, 1)))
+    C = rng.standard_normal((k1, k2))
+    y_tc = lincomb(ctx, X, C, tc=True)
+    y_64 = lincomb(ctx, X, C, tc=False)
+    scale = np.abs(X) @ np.abs(C)
+    assert np.max(np.abs(y_tc - y_64) / scale) < 1e-14
+    for r in (0, n // 2, n - 1):
+        for j in (0, k2 - 1):
+            ex = exact_dot(X[r], C[:, j])
+            assert abs(y_tc[r, j] - ex) <= 4e-16 * abs(ex) + 2.0 ** -51 * scale[r, j]
+
+
+def test_tensor_lincomb_exact_on_integers(ctx):
+    rng = np.random.default_rng(8)
+    X = rng.integers(-1000, 1000, size=(3000, 140)).astype(np.float64)
+    C = rng.integers(-1000, 1000, size=(140, 40)).astype(np.float64)
+    assert np.array_equal(lincomb(ctx, X, C), X @ C)
+
+
+def test_tensor_lincomb_wide_dynamic_range(ctx):
+    """Row entries spanning 2^-40 .. 1: errors bounded by the row and column scales."""
+    rng = np.random.default_rng(9)
+    X = rng.standard_normal((2000, 45)) * np.exp2(-40 * rng.random((2000, 45)))
+    C = rng.standard_normal((45, 9)) * np.exp2(-30 * rng.random((45, 9)))
+    y = lincomb(ctx, X, C)
+    for r in range(0, 2000, 97):
+        for j in range(9):
+            ex = exact_dot(X[r], C[:, j])
+            bound = 45 * 2.0 ** -53 * np.max(np.abs(X[r])) * np.max(np.abs(C[:, j])) + 2.0 ** -52 * abs(ex)
+            assert abs(y[r, j] - ex) <= bound
+
+
+def test_tensor_lincomb_zero_rows_and_columns(ctx):
+    rng = np.random.default_rng(10)
+    X = rng.standard_normal((700, 20))
+    X[5] = 0.0
+    X[:, 3] = 0.0
+    C = rng.standard_normal((20, 6))
+    C[:, 2] = 0.0
+    y = lincomb(ctx, X, C)
+    assert np.all(y[5] == 0.0) and np.all(y[:, 2] == 0.0)
+    np.testing.assert_allclose(y, X @ C, rtol=0, atol=1e-13 * np.max(np.abs(X) @ np.abs(C)))
+
+
+def oz_lincomb_bound(X, C):
+    """Elementwise error guarantee of the split product: with g_i the exponent of
+    row i of C, Xt = X 2^g and Ct = 2^-g C are split against their row and column
+    maxima (relative rounding 2^-54 of the maximum each) and the dropped digit
+    levels add less than 2^-51 of maxX*maxC per term."""
+    g = np.frexp(np.max(np.abs(C), axis=1))[1].astype(np.float64)
+    Xt, Ct = X * np.exp2(g), C * np.exp2(-g)[:, None]
+    mx, mc = np.max(np.abs(Xt), axis=1), np.max(np.abs(Ct), axis=0)
+    k1 = X.shape[1]
+    return 2.0 ** -53 * (mx[:, None] * np.sum(np.abs(Ct), axis=0)[None, :] +
+                         np.sum(np.abs(Xt), axis=1)[:, None] * mc[None, :]) + \
+        2.0 ** -50 * k1 * mx[:, None] * mc[None, :]
+
+
+def test_tensor_lincomb_compensating_scales(ctx):
+    """Columns of X spanning 2^-30 .. 1 with C scaling them back up (the W R^-1 of a
+    Cholesky QR after projection): the inner dimension is equilibrated, so errors
+    stay at FP64 level normwise and within the split's guarantee elementwise."""
+    rng = np.random.default_rng(11)
+    n, k1, k2 = 5000, 40, 40
+    colscale = np.exp2(-30 * rng.random(k1))
+    X = rng.standard_normal((n, k1)) * colscale
+    C = np.triu(rng.standard_normal((k1, k2))) / colscale[:, None]
+    y_tc = lincomb(ctx, X, C, tc=True)
+    y_64 = lincomb(ctx, X, C, tc=False)
+    scale = np.abs(X) @ np.abs(C)
+    col_err = np.linalg.norm(y_tc - y_64, axis=0) / np.linalg.norm(scale, axis=0)
+    assert np.max(col_err) < 1e-14
+    bound = oz_lincomb_bound(X, C)
+    for r in (0, 1234, n - 1):
+        for j in (0, 17, k2 - 1):
+            ex = exact_dot(X[r], C[:, j])
+            assert abs(y_tc[r, j] - ex) <= 2.0 ** -52 * abs(ex) + bound[r, j]
