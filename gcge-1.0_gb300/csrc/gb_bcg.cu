@@ -289,7 +289,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
         double *W = (double *)take((size_t)n * ld * vec);
         (void)W;
         // R = RHS - A X, in place in RHS (the reference overwrites RHS with the residual)
-        int st = gb_spmm(ctx, A, X, ldx, RHS, ldr, k, -1.0, nullptr, 1.0, nullptr);
+        int st = a->rhs_is_residual ? 0 : gb_spmm(ctx, A, X, ldx, RHS, ldr, k, -1.0, nullptr, 1.0, nullptr);
         if (st) return st;
         // P and W use the compact ld; R and X keep their own ld through the copies below
         if (ldr == ld && ldx == ld) {
@@ -321,7 +321,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     float *W = (float *)take((size_t)n * ld * vec);
     if ((size_t)(w - (char *)work) > work_bytes) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     int st;
-    if ((st = gb_spmm(ctx, A, X, ldx, RHS, ldr, k, -1.0, nullptr, 1.0, nullptr))) return st;
+    if (!a->rhs_is_residual && (st = gb_spmm(ctx, A, X, ldx, RHS, ldr, k, -1.0, nullptr, 1.0, nullptr))) return st;
     if ((st = gb_convert_d2f(ctx, n, k, RHS, ldr, R, ld))) return st;
     if (cudaMemsetAsync(D, 0, (size_t)n * ld * sizeof(float), ctx->stream) != cudaSuccess)
         return gb_fail(ctx, GCGE_GPU_ERR_CUDA);

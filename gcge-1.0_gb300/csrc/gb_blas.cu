@@ -79,7 +79,7 @@ k_spmm(int n, const int *__restrict__ rp, const int *__restrict__ ci, const VT *
     }
 }
 
-// Vectorised SpMM: a group of L lanes (L = 8, 16 or 32) owns one row and VW =
+// Vectorised SpMM: a group of L lanes (L = 4, 8, 16 or 32) owns one row and VW =
 // 16 / sizeof(T) consecutive columns per lane, so each nonzero gathers its block
 // row of X with one 16-byte load per lane; 32 / L rows per warp. The group loads
 // up to L (column, value) pairs at once and broadcasts them with group-masked
@@ -128,7 +128,9 @@ k_spmm_vec(int n, const int *__restrict__ rp, const int *__restrict__ ci, const 
                     const T *xs = reinterpret_cast<const T *>(&xv);
 #pragma unroll
                     for (int q = 0; q < VW; ++q) acc[q] = fma(aa, xs[q], acc[q]);
-                } else {
+                } else if (c < kact) {
+                    // ragged tail (k not a multiple of VW); lanes past the last column
+                    // skip both branches so the warp issues the vector FMAs only once
 #pragma unroll
                     for (int q = 0; q < VW; ++q)
                         if (c + q < kact) acc[q] = fma(aa, __ldg(xr + q), acc[q]);
@@ -145,12 +147,12 @@ k_spmm_vec(int n, const int *__restrict__ rp, const int *__restrict__ ci, const 
     }
 }
 
-// lanes per row for the vectorised SpMM: the smallest of 8/16/32 covering k
+// lanes per row for the vectorised SpMM: the smallest of 4/8/16/32 covering k
 template <typename T>
 static int spmm_vec_lanes(int k)
 {
     const int need = (k + (16 / (int)sizeof(T)) - 1) / (16 / (int)sizeof(T));
-    return need <= 8 ? 8 : (need <= 16 ? 16 : 32);
+    return need <= 4 ? 4 : (need <= 8 ? 8 : (need <= 16 ? 16 : 32));
 }
 
 static bool aligned16(const void *p, long ld, size_t es)
@@ -196,7 +198,10 @@ extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X
             const int L = spmm_vec_lanes<double>(k);
             const long warps = ((long)A->n * L + 31) / 32;
             const int grid = ceil_div_l(warps * 32, 256);
-            if (L == 8)
+            if (L == 4)
+                GB_LAUNCH(ctx, (k_spmm_vec<double, 4>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
+                          alpha, alpha_col, beta, ncols_dev);
+            else if (L == 8)
                 GB_LAUNCH(ctx, (k_spmm_vec<double, 8>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
                           alpha, alpha_col, beta, ncols_dev);
             else if (L == 16)
@@ -231,7 +236,10 @@ extern "C" int gb_spmm32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const float *
             const int L = spmm_vec_lanes<float>(k);
             const long warps = ((long)A->n * L + 31) / 32;
             const int grid = ceil_div_l(warps * 32, 256);
-            if (L == 8)
+            if (L == 4)
+                GB_LAUNCH(ctx, (k_spmm_vec<float, 4>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y, ldy, k,
+                          1.0f, (const double *)nullptr, 0.0f, ncols_dev);
+            else if (L == 8)
                 GB_LAUNCH(ctx, (k_spmm_vec<float, 8>), grid, 256, 0, A->n, A->rp, A->ci, A->v32, X, ldx, Y, ldy, k,
                           1.0f, (const double *)nullptr, 0.0f, ncols_dev);
             else if (L == 16)
@@ -296,20 +304,37 @@ extern "C" int gb_axpby(gcge_gpu_ctx *ctx, int n, int k, double a, const double 
     return GCGE_GPU_OK;
 }
 
-__global__ void k_gather_cols(int n, int k, const double *__restrict__ X, long ldx, const int *__restrict__ idx,
-                              double *__restrict__ Y, long ldy, const double *__restrict__ eval, int mode)
+// per-column source index and scale of a gather, staged once per block in
+// shared memory (scale 1, or 1 / lambda of the column when |lambda| > 1)
+__device__ __forceinline__ void gather_setup(int k, const int *idx, const double *eval, int mode, int *si,
+                                             double *ss)
 {
-    const int lane = threadIdx.x & 31;
-    ROWS_BY_WARP(n, r)
-    for (int c = lane; c < k; c += 32) {
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
         const int src = idx ? idx[c] : c;
+        si[c] = src;
         double s = 1.0;
         if (mode == 1) {
             const double l = eval[src];
             s = fabs(l) <= 1.0 ? 1.0 : 1.0 / l;
         }
-        const double x = X[r * ldx + src];
-        Y[r * ldy + c] = (mode == 1 && s != 1.0) ? s * x : x;
+        ss[c] = s;
+    }
+    __syncthreads();
+}
+
+__global__ void k_gather_cols(int n, int k, const double *__restrict__ X, long ldx, const int *__restrict__ idx,
+                              double *__restrict__ Y, long ldy, const double *__restrict__ eval, int mode)
+{
+    extern __shared__ double gsm[];
+    double *ss = gsm;
+    int *si = (int *)(gsm + k);
+    gather_setup(k, idx, eval, mode, si, ss);
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) {
+        const double s = ss[c];
+        const double x = X[r * ldx + si[c]];
+        Y[r * ldy + c] = s != 1.0 ? s * x : x;
     }
 }
 
@@ -317,8 +342,39 @@ extern "C" int gb_gather_cols(gcge_gpu_ctx *ctx, int n, int k, const double *X, 
                               double *Y, long ldy, const double *eval_dev, int mode)
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
-    GB_LAUNCH(ctx, k_gather_cols, row_grid(ctx, n), 256, 0, n, k, X, ldx, idx_dev, Y, ldy,
+    if (k > 4096) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    GB_LAUNCH(ctx, k_gather_cols, row_grid(ctx, n), 256, (size_t)k * 12, n, k, X, ldx, idx_dev, Y, ldy,
               eval_dev, mode);
+    return GCGE_GPU_OK;
+}
+
+// initial residual of the correction equation from products already formed:
+// R[:, c] = s_c (lam_c BX[:, bi[c]] - AX[:, ai[c]]) with the scale of the initial
+// guess, s_c = 1 if |lam_c| <= 1 else 1 / lam_c
+__global__ void k_w_residual(int n, int k, const double *__restrict__ AX, long ldax, const int *__restrict__ ai,
+                             const double *__restrict__ BX, long ldbx, const int *__restrict__ bi,
+                             const double *__restrict__ lam, double *__restrict__ R, long ldr)
+{
+    extern __shared__ double gsm[];
+    double *ss = gsm;
+    int *si = (int *)(gsm + k);
+    gather_setup(k, nullptr, lam, 1, si, ss);
+    const int lane = threadIdx.x & 31;
+    ROWS_BY_WARP(n, r)
+    for (int c = lane; c < k; c += 32) {
+        const double v = lam[c] * BX[r * ldbx + bi[c]] - AX[r * ldax + ai[c]];
+        R[r * ldr + c] = ss[c] != 1.0 ? ss[c] * v : v;
+    }
+}
+
+extern "C" int gb_w_residual(gcge_gpu_ctx *ctx, int n, int k, const double *AX, long ldax, const int *ai,
+                             const double *BX, long ldbx, const int *bi, const double *lam, double *R, long ldr)
+{
+    if (n <= 0 || k <= 0) return GCGE_GPU_OK;
+    if (k > 4096) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    GB_PROF(ctx, GB_K_BLAS1, 24.0 * n * k, 3.0 * n * k);
+    GB_LAUNCH(ctx, k_w_residual, row_grid(ctx, n), 256, (size_t)k * 12, n, k, AX, ldax, ai, BX, ldbx, bi, lam, R,
+              ldr);
     return GCGE_GPU_OK;
 }
 

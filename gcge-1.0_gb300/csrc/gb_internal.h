@@ -139,10 +139,14 @@ int gb_frobenius(gcge_gpu_ctx *ctx, int m, int n, const double *a, int lda, doub
 typedef struct {
     int n, k, max_it, precision;
     double rate;
+    int rhs_is_residual;       /* RHS already holds RHS - A X: skip the initial product */
 } gb_bcg_args;
 int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, long ldr, double *X, long ldx,
            const gb_bcg_args *args, void *work, size_t work_bytes);
 size_t gb_bcg_work_bytes(int n, int k, int precision);
+/* R[:, c] = s_c (lam_c BX[:, bi[c]] - AX[:, ai[c]]), s_c = 1 if |lam_c| <= 1 else 1 / lam_c */
+int gb_w_residual(gcge_gpu_ctx *ctx, int n, int k, const double *AX, long ldax, const int *ai, const double *BX,
+                  long ldbx, const int *bi, const double *lam, double *R, long ldr);
 
 /* ------------------------------------------------------------ gb_dense.cu */
 /* C = alpha op(A) op(B) + beta C, small column-major matrices on the device */

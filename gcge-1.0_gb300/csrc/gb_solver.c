@@ -61,10 +61,13 @@ typedef struct {
     size_t bcg_bytes;
     /* device small dense */
     double *H, *C, *Ctmp, *AApp, *Gs, *Ts, *chol_work, *eval_d, *eig_work, *res_d, *lam_d, *dsmall;
-    int *unlock_d, *kept_d, *info_d;
+    int *unlock_d, *kept_d, *info_d, *pos_d;
     /* host */
     double *eval_h, *res_h, *resv;
-    int *unlock_h;
+    int *unlock_h, *pos_h;
+    /* S2 = A X and S3 = B X for the unlock list the last convergence check saw;
+     * pos_h[j] = position of the j-th unlocked column in that list */
+    int conv_products;
     /* state (GCGE_WORKSPACE / GCGE_PARA members) */
     int dim_x, dim_xp, dim_xpw, last_dim_xpw, last_dim_x, unconv_bs, num_unlock, num_iter;
     double max_res, min_res, sum_res, conv_omega_norm, zero_tol;
@@ -222,9 +225,13 @@ static int check_conv(gcg_t *g)
         if (j == 0) { max_res = r; min_res = r; }
         else { if (r > max_res) max_res = r; if (r < min_res) min_res = r; }
         if (r > g->p.ev_tol) {
+            g->pos_h[unconv] = j;
             g->unlock_h[unconv++] = i;
             if (j > max_conv_idx + 8) {
-                for (int k = j + 1; k < nu; ++k) g->unlock_h[unconv++] = g->unlock_h[k];
+                for (int k = j + 1; k < nu; ++k) {
+                    g->pos_h[unconv] = k;
+                    g->unlock_h[unconv++] = g->unlock_h[k];
+                }
                 j = nu + 1;
             }
         } else {
@@ -237,8 +244,13 @@ static int check_conv(gcg_t *g)
     g->min_res = min_res;
     g->sum_res = sum_res;
     g->num_iter += 1;
-    if (unconv > 0)
+    if (unconv > 0) {
         CTRY(cudaMemcpyAsync(g->unlock_d, g->unlock_h, sizeof(int) * unconv, cudaMemcpyHostToDevice, ctx->stream));
+        CTRY(cudaMemcpyAsync(g->pos_d, g->pos_h, sizeof(int) * unconv, cudaMemcpyHostToDevice, ctx->stream));
+        /* the copies read pos_h / unlock_h before the next host update: order them */
+        CTRY(cudaStreamSynchronize(ctx->stream));
+    }
+    g->conv_products = nu > 0;
     if (g->p.print_level > 0)
         printf("num_unlock(%3d) = %3d; max_res(%3d) = %e; min_res(%3d) = %e;\n", g->num_iter, g->num_unlock,
                g->num_iter, max_res, g->num_iter, min_res);
@@ -258,14 +270,29 @@ static int compute_w(gcg_t *g)
     double *W = g->V + ws;
     TRY(gb_gather_cols(ctx, n, wl, g->V, g->ldv, g->unlock_d, W, g->ldv, g->eval_d, 1));
     TRY(gb_select(ctx, wl, g->eval_d, g->unlock_d, g->lam_d));
-    if (g->B) TRY(gb_spmm(ctx, g->B, W, g->ldv, g->S1, g->lds, wl, 1.0, g->lam_d, 0.0, NULL));
-    else TRY(gb_scale_cols(ctx, n, wl, W, g->ldv, g->lam_d, g->S1, g->lds));
     gb_bcg_args a;
     a.n = n;
     a.k = wl;
     a.max_it = g->p.cg_max_it;
     a.precision = g->p.precision;
     a.rate = g->p.cg_rate;
+    a.rhs_is_residual = 0;
+    if (g->conv_products) {
+        /* the convergence check left A x (S2) and B x (S3) of these columns: the
+         * initial residual l B w - A w, w = s x, is s (l B x - A x) without a product */
+        if (g->B)
+            TRY(gb_w_residual(ctx, n, wl, g->S2, g->lds, g->pos_d, g->S3, g->lds, g->pos_d, g->lam_d, g->S1,
+                              g->lds));
+        else
+            TRY(gb_w_residual(ctx, n, wl, g->S2, g->lds, g->pos_d, g->V, g->ldv, g->unlock_d, g->lam_d, g->S1,
+                              g->lds));
+        a.rhs_is_residual = 1;
+    } else if (g->B) {
+        TRY(gb_spmm(ctx, g->B, W, g->ldv, g->S1, g->lds, wl, 1.0, g->lam_d, 0.0, NULL));
+    } else {
+        TRY(gb_scale_cols(ctx, n, wl, W, g->ldv, g->lam_d, g->S1, g->lds));
+    }
+    g->conv_products = 0;
     TRY(gb_bcg(ctx, g->A, g->S1, g->lds, W, g->ldv, &a, g->bcg_work, g->bcg_bytes));
     return 0;
 fail:
@@ -344,7 +371,7 @@ static void gcg_free(gcg_t *g)
 {
     void *dev[] = {g->V, g->S1, g->S2, g->S3, g->bcg_work, g->H, g->C, g->Ctmp, g->AApp, g->Gs, g->Ts,
                    g->chol_work, g->eval_d, g->eig_work, g->res_d, g->lam_d, g->dsmall, g->unlock_d, g->kept_d,
-                   g->info_d};
+                   g->info_d, g->pos_d};
     for (size_t i = 0; i < sizeof(dev) / sizeof(dev[0]); ++i)
         if (dev[i]) cudaFree(dev[i]);
     gb_orth_ws_free(&g->ows);
@@ -352,6 +379,7 @@ static void gcg_free(gcg_t *g)
     free(g->res_h);
     free(g->resv);
     free(g->unlock_h);
+    free(g->pos_h);
     for (int i = 0; i < 128; ++i)
         if (g->tm.ev[i]) cudaEventDestroy(g->tm.ev[i]);
 }
@@ -408,7 +436,8 @@ int GCGE_GPU_Solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat 
         dmalloc((void **)&g->eig_work, sizeof(double) * gb_syevx_work_doubles((int)vs)) ||
         dmalloc((void **)&g->res_d, sizeof(double) * 3 * (nev + 8)) || dmalloc((void **)&g->lam_d, sizeof(double) * (vs + 8)) ||
         dmalloc((void **)&g->dsmall, sizeof(double) * 64) || dmalloc((void **)&g->unlock_d, sizeof(int) * vs) ||
-        dmalloc((void **)&g->kept_d, sizeof(int) * 4) || dmalloc((void **)&g->info_d, sizeof(int) * 4)) {
+        dmalloc((void **)&g->kept_d, sizeof(int) * 4) || dmalloc((void **)&g->info_d, sizeof(int) * 4) ||
+        dmalloc((void **)&g->pos_d, sizeof(int) * vs)) {
         st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
         goto fail;
     }
@@ -419,7 +448,8 @@ int GCGE_GPU_Solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat 
     g->res_h = (double *)calloc(3 * (nev + 8), sizeof(double));
     g->resv = (double *)calloc(nev, sizeof(double));
     g->unlock_h = (int *)calloc(vs, sizeof(int));
-    if (!g->eval_h || !g->res_h || !g->resv || !g->unlock_h) { st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM); goto fail; }
+    g->pos_h = (int *)calloc(vs, sizeof(int));
+    if (!g->eval_h || !g->res_h || !g->resv || !g->unlock_h || !g->pos_h) { st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM); goto fail; }
     CTRY(cudaMemsetAsync(g->V, 0, sizeof(double) * (size_t)n * g->ldv, ctx->stream));
     CTRY(cudaMemsetAsync(g->eval_d, 0, sizeof(double) * vs, ctx->stream));
     CTRY(cudaMemsetAsync(g->info_d, 0, sizeof(int), ctx->stream));
