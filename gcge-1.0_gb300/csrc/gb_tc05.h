@@ -118,25 +118,33 @@ __device__ __forceinline__ void tc_mma_commit(uint32_t bar)
 
 // ---------------------------------------------------------------- error-free digit splitting
 // An FP64 entry x of a row (or column) with scale 2^e (|x| < 2^e over the row)
-// is the integer T = x 2^(54 - e), |T| <= 2^54, exact to 2^(e - 54). With the
-// bias B = 0x80808080808080, U = T + B lies in [0, 2^56) and its seven bytes
-// b_0 (least significant) .. b_6 give balanced digits b - 128 in [-128, 127]:
-//   x = sum_p (b_(6-p) - 128) 2^(-8p) 2^(e - 6),   p = 0 (most significant) .. 6.
-// Only integer operations touch x; every digit is exact in f16 (and bf16).
+// is the integer T = x 2^(53 - e) rounded to nearest, |T| <= 2^53, i.e. exact to
+// half a unit of 2^(e - 53). With the bias B = 0x80808080808080, U = T + B lies
+// in [0, 2^56) and its seven bytes b_0 (least significant) .. b_6 give balanced
+// digits d_p = b_(6-p) - 128:
+//   x = sum_p d_p 2^(-8p) 2^(e - 5),   p = 0 (most significant) .. 6,
+// with d_0 in [-32, 32] and d_1 .. d_6 in [-128, 127]. Only integer operations
+// touch x; every digit is exact in f16 (and bf16).
+//
+// Exact accumulation bound: the digit products of level L = p + q are at most
+// 2^12 for the two pairs with p = 0 or q = 0 and 2^14 for the others, so a
+// level sums to at most 2^13 + 5 * 2^14 per term (L = 6) and stays below 2^24
+// -- an exact FP32 integer -- for up to OZ_EXACT_TERMS terms.
 #define OZ_DIGITS 7
 #define OZ_NO_EXP (-2000)          // scale of an all-zero row or column
 #define OZ_BIAS 0x80808080808080ULL
+#define OZ_EXACT_TERMS 186
+#define OZ_SCALE_OFFSET 10         // a digit product of level 0 carries 2^(e + f - 10)
 
 __device__ __forceinline__ unsigned long long oz_bias(double x, int e)
 {
     const long long b = __double_as_longlong(x);
     const int ex = (int)((b >> 52) & 0x7ff);
     long long T = 0;
-    if (ex) {
+    const int r = e + 1022 - ex;                          // T = mant 2^-r, r >= 0
+    if (ex && r < 60) {
         const long long mant = (b & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
-        const int sh = ex - 1021 - e;                    // T = mant 2^sh, sh <= 1
-        if (sh >= 0) T = mant << sh;
-        else if (sh > -60) T = (mant + (1LL << (-sh - 1))) >> (-sh);
+        T = (mant + ((1LL << r) >> 1)) >> r;
         if (b < 0) T = -T;
     }
     return (unsigned long long)T + OZ_BIAS;
@@ -162,10 +170,13 @@ __device__ __forceinline__ uint32_t oz_pack(unsigned long long u0, unsigned long
 }
 
 // ---------------------------------------------------------------- exact integer -> FP64
-// (hi 2^32 + lo) 2^(s - 48) rounded once to nearest-even
+// (hi 2^SH + lo) 2^(s - 16 - SH) rounded once to nearest-even, s = e + f -
+// OZ_SCALE_OFFSET: hi holds levels 0-2 in units of 2^-16, lo the lower levels in
+// units of 2^-(16 + SH) (SH = 32 for levels 3-6, 40 for levels 3-7)
+template <int SH>
 __device__ __forceinline__ double oz_to_double(long long hi, long long lo, int s)
 {
-    __int128 z = ((__int128)hi << 32) + (__int128)lo;
+    __int128 z = ((__int128)hi << SH) + (__int128)lo;
     if (z == 0) return 0.0;
     unsigned long long sign = 0;
     if (z < 0) {
@@ -175,7 +186,7 @@ __device__ __forceinline__ double oz_to_double(long long hi, long long lo, int s
     const unsigned __int128 u = (unsigned __int128)z;
     const unsigned long long zh = (unsigned long long)(u >> 64), zl = (unsigned long long)u;
     const int nb = zh ? 128 - __clzll((long long)zh) : 64 - __clzll((long long)zl);
-    int E = nb - 1 + s - 48;
+    int E = nb - 1 + s - 16 - SH;
     unsigned long long m;
     if (nb <= 53) {
         m = zl << (53 - nb);
@@ -191,20 +202,20 @@ __device__ __forceinline__ double oz_to_double(long long hi, long long lo, int s
             ++E;
         }
     }
-    if (E < -1022 || E > 1023) {                   // outside the normal range: scale in FP64
-        const double v = ldexp((double)hi, s - 16) + ldexp((double)lo, s - 48);
-        return v;
-    }
+    if (E < -1022 || E > 1023)                     // outside the normal range: scale in FP64
+        return ldexp((double)hi, s - 16) + ldexp((double)lo, s - 16 - SH);
     return __longlong_as_double((long long)(sign | ((unsigned long long)(E + 1023) << 52) |
                                             (m & ((1ull << 52) - 1))));
 }
 
-// levels 0..6 (exact FP32 integers) -> hi (levels 0-2, units 2^-16) and
-// lo (levels 3-6, units 2^-48) of one output
-__device__ __forceinline__ void oz_levels_to_int(const float v[OZ_DIGITS], long long &hi, long long &lo)
+// levels (exact FP32 integers) -> hi (levels 0-2, units 2^-16) and lo (levels
+// 3 .. LEVELS-1 in units of the lowest level) of one output
+template <int LEVELS>
+__device__ __forceinline__ void oz_levels_to_int(const float *v, long long &hi, long long &lo)
 {
     hi = ((long long)__float2int_rn(v[0]) << 16) + ((long long)__float2int_rn(v[1]) << 8) +
          (long long)__float2int_rn(v[2]);
-    lo = ((long long)__float2int_rn(v[3]) << 24) + ((long long)__float2int_rn(v[4]) << 16) +
-         ((long long)__float2int_rn(v[5]) << 8) + (long long)__float2int_rn(v[6]);
+    lo = 0;
+#pragma unroll
+    for (int L = 3; L < LEVELS; ++L) lo += (long long)__float2int_rn(v[L]) << (8 * (LEVELS - 1 - L));
 }

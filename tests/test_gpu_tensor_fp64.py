@@ -100,6 +100,20 @@ def lincomb(ctx, X, C, tc=True):
         ctx.tensor_emulation(True)
 
 
+def oz_lincomb_bound(X, C):
+    """Elementwise error guarantee of the split product: with g_i the exponent of
+    row i of C, Xt = X 2^g and Ct = 2^-g C are split against their row and column
+    maxima (rounding below 2^-53 of the maximum each) and the dropped digit
+    levels add less than 2^-54 of maxX*maxC per term."""
+    g = np.frexp(np.max(np.abs(C), axis=1))[1].astype(np.float64)
+    Xt, Ct = X * np.exp2(g), C * np.exp2(-g)[:, None]
+    mx, mc = np.max(np.abs(Xt), axis=1), np.max(np.abs(Ct), axis=0)
+    k1 = X.shape[1]
+    return 2.0 ** -53 * (mx[:, None] * np.sum(np.abs(Ct), axis=0)[None, :] +
+                         np.sum(np.abs(Xt), axis=1)[:, None] * mc[None, :]) + \
+        2.0 ** -54 * k1 * mx[:, None] * mc[None, :]
+
+
 @pytest.mark.parametrize("n,k1,k2", [(1000, 37, 21), (100003, 178, 50), (5000, 64, 64), (20000, 100, 130),
                                      (77, 3, 5), (300, 1, 1), (4099, 129, 17)])
 def test_tensor_lincomb_matches_fp64_pipe(ctx, n, k1, k2):
@@ -110,10 +124,11 @@ def test_tensor_lincomb_matches_fp64_pipe(ctx, n, k1, k2):
     y_64 = lincomb(ctx, X, C, tc=False)
     scale = np.abs(X) @ np.abs(C)
     assert np.max(np.abs(y_tc - y_64) / scale) < 1e-14
+    bound = oz_lincomb_bound(X, C)
     for r in (0, n // 2, n - 1):
         for j in (0, k2 - 1):
             ex = exact_dot(X[r], C[:, j])
-            assert abs(y_tc[r, j] - ex) <= 4e-16 * abs(ex) + 2.0 ** -51 * scale[r, j]
+            assert abs(y_tc[r, j] - ex) <= 2.0 ** -52 * abs(ex) + bound[r, j]
 
 
 def test_tensor_lincomb_exact_on_integers(ctx):
@@ -146,20 +161,6 @@ def test_tensor_lincomb_zero_rows_and_columns(ctx):
     y = lincomb(ctx, X, C)
     assert np.all(y[5] == 0.0) and np.all(y[:, 2] == 0.0)
     np.testing.assert_allclose(y, X @ C, rtol=0, atol=1e-13 * np.max(np.abs(X) @ np.abs(C)))
-
-
-def oz_lincomb_bound(X, C):
-    """Elementwise error guarantee of the split product: with g_i the exponent of
-    row i of C, Xt = X 2^g and Ct = 2^-g C are split against their row and column
-    maxima (relative rounding 2^-54 of the maximum each) and the dropped digit
-    levels add less than 2^-51 of maxX*maxC per term."""
-    g = np.frexp(np.max(np.abs(C), axis=1))[1].astype(np.float64)
-    Xt, Ct = X * np.exp2(g), C * np.exp2(-g)[:, None]
-    mx, mc = np.max(np.abs(Xt), axis=1), np.max(np.abs(Ct), axis=0)
-    k1 = X.shape[1]
-    return 2.0 ** -53 * (mx[:, None] * np.sum(np.abs(Ct), axis=0)[None, :] +
-                         np.sum(np.abs(Xt), axis=1)[:, None] * mc[None, :]) + \
-        2.0 ** -50 * k1 * mx[:, None] * mc[None, :]
 
 
 def test_tensor_lincomb_compensating_scales(ctx):
