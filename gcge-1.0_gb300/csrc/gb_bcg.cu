@@ -233,6 +233,277 @@ extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
     return blocks + state + 16 * 256;   // every sub-buffer is aligned to 256 bytes (10 of them)
 }
 
+// ---------------------------------------------------------------- FP32 rounds, fused
+// The FP32 (mixed-precision) rounds run on float4 kernels with a fixed grid of
+// VB_G blocks: block b always owns the same rows, so the per-block partial sums
+// and their fixed-order column sums are deterministic. A round is five launches:
+// p update, SpMM with the p.w partials in its epilogue, alpha, x/r update with
+// the r.r partials, beta and the active count.
+#define VB_THREADS 256
+#define VB_ROWS 16                                   // row slots of a block, 64 columns per column tile
+
+static int vec_blocks(gcge_gpu_ctx *ctx, int n)
+{
+    long g = cdiv(n > 0 ? n : 1, RED_ROWS), cap = (long)ctx->num_sms * 6;
+    return (int)(g < cap ? g : cap);
+}
+
+// sum the per-thread column partials s[4] (thread (rs, cg) holds columns
+// c0 + 4 cg .. +3 of its row slot) over the row slots in a fixed order
+template <int SLOTS, int COLS>
+__device__ __forceinline__ void vb_block_reduce(const double s[4], int slot, int cg, int c0, int k, double *part)
+{
+    __shared__ double red[SLOTS][COLS + 1];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) red[slot][4 * cg + q] = s[q];
+    __syncthreads();
+    for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
+        double t = 0;
+        for (int r = 0; r < SLOTS; ++r) t += red[r][c];
+        if (c0 + c < k) part[(long)blockIdx.x * k + c0 + c] = t;
+    }
+}
+
+// p = r + beta p (p = r on the first round) on the active columns
+__global__ void __launch_bounds__(VB_THREADS)
+k_pupdate_v(int n, int k, const float *__restrict__ R, float *__restrict__ P, long ld,
+            const double *__restrict__ beta, const int *__restrict__ nact, int first)
+{
+    const int ka = min(*nact, k);
+    const int cg = threadIdx.x & 15, rs = threadIdx.x >> 4;
+    const int c0 = blockIdx.y * 64 + 4 * cg;
+    if (c0 >= ka) return;
+    float b[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) b[q] = (!first && c0 + q < ka) ? (float)beta[c0 + q] : 0.f;
+    const bool full = c0 + 4 <= ka;
+    for (long r = (long)blockIdx.x * VB_ROWS + rs; r < n; r += (long)gridDim.x * VB_ROWS) {
+        const float4 rv = *reinterpret_cast<const float4 *>(R + r * ld + c0);
+        float4 *pp = reinterpret_cast<float4 *>(P + r * ld + c0);
+        if (first) {                               // p = r: the old p (uninitialised) is not read
+            if (full) {
+                *pp = rv;
+            } else {
+                float *pe = reinterpret_cast<float *>(pp);
+                const float *re = &rv.x;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (c0 + q < ka) pe[q] = re[q];
+            }
+            continue;
+        }
+        float4 pv = *pp;
+        if (full) {
+            pv.x = rv.x + b[0] * pv.x; pv.y = rv.y + b[1] * pv.y;
+            pv.z = rv.z + b[2] * pv.z; pv.w = rv.w + b[3] * pv.w;
+        } else {
+            float *pe = &pv.x;
+            const float *re = &rv.x;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (c0 + q < ka) pe[q] = re[q] + b[q] * pe[q];
+        }
+        *pp = pv;
+    }
+}
+
+// x += alpha p, r -= alpha w on the active columns, with block partials of r.r
+// (FP32 products summed over runs of 8 rows, the runs summed in FP64)
+__global__ void __launch_bounds__(VB_THREADS)
+k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const float *__restrict__ P,
+              const float *__restrict__ W, long ld, const double *__restrict__ alpha, const int *__restrict__ nact,
+              double *__restrict__ part)
+{
+    const int ka = min(*nact, k);
+    const int cg = threadIdx.x & 15, rs = threadIdx.x >> 4;
+    const int c0 = blockIdx.y * 64 + 4 * cg;
+    double s[4] = {0, 0, 0, 0};
+    if (c0 < ka) {
+        float a[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = c0 + q < ka ? (float)alpha[c0 + q] : 0.f;
+        float run[4] = {0, 0, 0, 0};
+        int cnt = 0;
+        for (long r = (long)blockIdx.x * VB_ROWS + rs; r < n; r += (long)gridDim.x * VB_ROWS) {
+            const long o = r * ld + c0;
+            float4 xv = *reinterpret_cast<const float4 *>(X + o);
+            float4 rv = *reinterpret_cast<const float4 *>(R + o);
+            const float4 pv = *reinterpret_cast<const float4 *>(P + o);
+            const float4 wv = *reinterpret_cast<const float4 *>(W + o);
+            float *xe = &xv.x, *re = &rv.x;
+            const float *pe = &pv.x, *we = &wv.x;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                xe[q] = xe[q] + a[q] * pe[q];      // a = 0 leaves inactive columns unchanged
+                re[q] = re[q] - a[q] * we[q];
+                run[q] = fmaf(re[q], re[q], run[q]);
+            }
+            *reinterpret_cast<float4 *>(X + o) = xv;
+            *reinterpret_cast<float4 *>(R + o) = rv;
+            if (++cnt == 8) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) { s[q] += (double)run[q]; run[q] = 0.f; }
+                cnt = 0;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s[q] += (double)run[q];
+    }
+    vb_block_reduce<VB_ROWS, 64>(s, rs, cg, blockIdx.y * 64, ka, part);
+}
+
+// W = A P (FP32, the first nact columns) and block partials of p.w: L lanes per
+// row, 4 columns per lane, 256 / L rows per block pass; grid-stride over rows
+template <int L>
+__global__ void __launch_bounds__(VB_THREADS)
+k_spmm32_dot(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+             const float *__restrict__ P, float *__restrict__ W, long ld, int k, const int *__restrict__ nact,
+             double *__restrict__ part)
+{
+    constexpr int RPB = VB_THREADS / L;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / L, sl = lane % L;
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (sub * L));
+    const int slot = warp * (32 / L) + sub;
+    const int kact = min(*nact, k);
+    const int c = 4 * sl;
+    double s[4] = {0, 0, 0, 0};
+    float run[4] = {0, 0, 0, 0};
+    int cnt = 0;
+    if (kact > 0)
+        for (long row = (long)blockIdx.x * RPB + slot; row < n; row += (long)gridDim.x * RPB) {
+            const int beg = rp[row], end = rp[row + 1];
+            float acc[4] = {0, 0, 0, 0};
+            for (int base = beg; base < end; base += L) {
+                const int e = base + sl;
+                int j = 0;
+                float a = 0.f;
+                if (e < end) { j = __ldg(ci + e); a = __ldg(val + e); }
+                const int m = min(L, end - base);
+#pragma unroll 4
+                for (int t = 0; t < m; ++t) {
+                    const int jj = __shfl_sync(gmask, j, t, L);
+                    const float aa = __shfl_sync(gmask, a, t, L);
+                    if (c < kact) {
+                        const float4 xv = __ldg(reinterpret_cast<const float4 *>(P + (long)jj * ld + c));
+                        acc[0] = fmaf(aa, xv.x, acc[0]); acc[1] = fmaf(aa, xv.y, acc[1]);
+                        acc[2] = fmaf(aa, xv.z, acc[2]); acc[3] = fmaf(aa, xv.w, acc[3]);
+                    }
+                }
+            }
+            if (c < kact) {
+                const long o = row * ld + c;
+                const float4 pv = *reinterpret_cast<const float4 *>(P + o);
+                const float *pe = &pv.x;
+                float4 *wp = reinterpret_cast<float4 *>(W + o);
+                if (c + 4 <= kact) {
+                    *wp = make_float4(acc[0], acc[1], acc[2], acc[3]);
+                } else {
+                    float *we = reinterpret_cast<float *>(wp);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (c + q < kact) we[q] = acc[q];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (c + q < kact) run[q] = fmaf(pe[q], acc[q], run[q]);
+                if (++cnt == 8) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) { s[q] += (double)run[q]; run[q] = 0.f; }
+                    cnt = 0;
+                }
+            }
+        }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s[q] += (double)run[q];
+    vb_block_reduce<RPB, 4 * L>(s, slot, sl, 0, kact, part);
+}
+
+// column sums of the block partials (one block per active column, fixed order)
+// and alpha[c] = rho2[c] / ptw[c]
+__global__ void __launch_bounds__(256)
+k_colsum_alpha(int nblk, int k, const double *__restrict__ part, const int *__restrict__ nact,
+               const double *__restrict__ rho2, double *__restrict__ ptw, double *__restrict__ alpha)
+{
+    __shared__ double sh[256];
+    const int c = blockIdx.x;
+    if (c >= *nact) return;
+    double s = 0;
+    for (int b = threadIdx.x; b < nblk; b += 256) s += part[(long)b * k + c];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ptw[c] = sh[0];
+        alpha[c] = rho2[c] / sh[0];
+    }
+}
+
+// column sums of the r.r partials (a warp per column, fixed order), then the
+// end-of-round update of k_finalize in the same block
+__global__ void __launch_bounds__(1024)
+k_colsum_finalize(int nblk, int k, const double *__restrict__ part, double *sums, double *rho1, double *rho2,
+                  const double *__restrict__ err, int *nact, double rate, double *beta)
+{
+    __shared__ int cnt;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ka = *nact;
+    if (threadIdx.x == 0) cnt = 0;
+    for (int c = warp; c < ka; c += 32) {
+        double s = 0;
+        for (int b = lane; b < nblk; b += 32) s += part[(long)b * k + c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) sums[c] = s;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        if (c < ka) {
+            const double s = sums[c];
+            rho1[c] = rho2[c];
+            rho2[c] = s;
+            beta[c] = s / rho1[c];   // the next round's beta (src/gcge_cg.c:645)
+        }
+        const double lerr = sqrt(fabs(rho2[c]));
+        if (lerr / err[c] >= rate) atomicAdd(&cnt, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *nact = cnt;
+}
+
+static int bcg_rounds32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, float *R, float *X, float *P, float *W, long ld,
+                        const gb_bcg_args *a, bcg_state *s)
+{
+    const int n = a->n, k = a->k, G = vec_blocks(ctx, n);
+    const int ctiles = (k + 63) / 64;
+    const int L = k <= 16 ? 4 : (k <= 32 ? 8 : (k <= 64 ? 16 : 32));
+    if (k > 128 || !A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    for (int it = 1; it < a->max_it; ++it) {
+        GB_PROF(ctx, GB_K_BCGVEC, 12.0 * n * k, 2.0 * n * k);
+        GB_LAUNCH(ctx, k_pupdate_v, dim3(G, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
+        ctx->spmm_launches++;
+        GB_PROF(ctx, GB_K_SPMM32, 8.0 * A->nnz + 4.0 * (A->n + 1) + 12.0 * A->n * k, 2.0 * A->nnz * k + 2.0 * A->n * k);
+        if (L == 4)
+            GB_LAUNCH(ctx, k_spmm32_dot<4>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
+        else if (L == 8)
+            GB_LAUNCH(ctx, k_spmm32_dot<8>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
+        else if (L == 16)
+            GB_LAUNCH(ctx, k_spmm32_dot<16>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
+        else
+            GB_LAUNCH(ctx, k_spmm32_dot<32>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
+        GB_LAUNCH(ctx, k_colsum_alpha, k, 256, 0, G, k, s->part, s->nact, s->rho2, s->ptw, s->alpha);
+        GB_PROF(ctx, GB_K_BCGVEC, 24.0 * n * k, 6.0 * n * k);
+        GB_LAUNCH(ctx, k_xr_update_v, dim3(G, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact,
+                  s->part);
+        GB_LAUNCH(ctx, k_colsum_finalize, 1, 1024, 0, G, k, s->part, s->sums, s->rho1, s->rho2, s->err, s->nact,
+                  a->rate, s->beta);
+    }
+    return GCGE_GPU_OK;
+}
+
 template <typename T>
 static int bcg_rounds(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, T *R, T *X, T *P, T *W, long ld,
                       const gb_bcg_args *a, bcg_state *s)
@@ -328,7 +599,8 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     GB_LAUNCH(ctx, k_dot_partial<float>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
     GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
     GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
-    if ((st = bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s))) return st;
+    if ((st = k <= 128 ? bcg_rounds32(ctx, A, R, D, P, W, ld, a, &s) : bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s)))
+        return st;
     GB_LAUNCH(ctx, k_add_f2d, row_grid(ctx, n), 256, 0, n, k, D, ld, X, ldx);
     return gb_convert_f2d(ctx, n, k, R, ld, RHS, ldr);
 }

@@ -28,8 +28,9 @@
 //    16 (w / 4));
 //  * hand-offs through mbarriers: full[b] (stage b written, 480 arrivals),
 //    empty[b] (MMAs of stage b done, tcgen05.commit), drained (TMEM read out,
-//    512 arrivals); every wait is bounded and reports a timeout through the
-//    context's device error word;
+//    512 arrivals), copied[b] (bulk copy of the pre-split planes of stage b);
+//    every wait is bounded and reports a timeout through the context's device
+//    error word;
 //  * the split warps load the next stage's FP64 values while the MMAs of the
 //    current one run.
 // k_lincomb_tc: Y = alpha X C + beta Y, M = 128 rows of X, K = columns of X,
@@ -87,10 +88,11 @@ extern "C" int gb_gram_reduce_launch(gcge_gpu_ctx *ctx, int k1, int k2, int nspl
 
 // shared header of both kernels
 struct tc_hdr {
-    uint64_t bar[5];             // full[2], empty[2], drained
+    uint64_t bar[7];             // full[2], empty[2], drained, copied[2] (bulk copies of a stage)
     uint32_t tmem;
     int flag;                    // a bounded wait ran out in this CTA
 };
+static_assert(sizeof(tc_hdr) <= 64, "header overlaps the scale arrays");
 
 __device__ __forceinline__ void tc_fail(tc_hdr *h, int *err)
 {
@@ -109,6 +111,8 @@ __device__ __forceinline__ void tc_setup(tc_hdr *h)
         tc_mbar_init(b + 16, 1);
         tc_mbar_init(b + 24, 1);
         tc_mbar_init(b + 32, TC_THREADS);
+        tc_mbar_init(b + 40, 1);
+        tc_mbar_init(b + 48, 1);
         h->flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -117,14 +121,15 @@ __device__ __forceinline__ void tc_setup(tc_hdr *h)
 // MMA issue of stage s (lane 0 of the MMA warp): wait for the stage's planes
 // (and, at the first stage of a chunk, for the previous chunk's drain), issue the
 // digit pairs with p + q < LEVELS x TC_KS / 16 K steps, commit to empty[buf]
-template <int LEVELS>
+template <int LEVELS, bool COPIED>
 __device__ __forceinline__ void tc_issue_stage(tc_hdr *h, uint32_t sbase, uint32_t tmem, int N, int s, int cs,
                                                int *commits, int *err)
 {
     const int buf = s & 1;
     const uint32_t full = tc_smem_addr(h->bar) + 8 * buf, empty = tc_smem_addr(h->bar) + 16 + 8 * buf;
-    const uint32_t drained = tc_smem_addr(h->bar) + 32;
+    const uint32_t drained = tc_smem_addr(h->bar) + 32, copied = tc_smem_addr(h->bar) + 40 + 8 * buf;
     bool ok = tc_mbar_wait(full, (s >> 1) & 1, TC_WAIT_NS);
+    if (COPIED && ok) ok = tc_mbar_wait(copied, (s >> 1) & 1, TC_WAIT_NS);
     if (ok && cs == 0 && s > 0) ok = tc_mbar_wait(drained, (commits[2] - 1) & 1, TC_WAIT_NS);
     if (!ok || *(volatile int *)&h->flag) {
         tc_fail(h, err);
@@ -176,14 +181,23 @@ __device__ __forceinline__ bool tc_wait_chunk(tc_hdr *h, int s, int *err)
     return true;
 }
 
-__device__ __forceinline__ void tc_release(tc_hdr *h, uint32_t tmem, int mma_warp, const int *commits)
+// copies: bulk copies issued per buffer by thread 0 (nullptr if none)
+__device__ __forceinline__ void tc_release(tc_hdr *h, uint32_t tmem, int mma_warp, const int *commits,
+                                           const int *copies)
 {
     __syncthreads();
-    if (mma_warp && (threadIdx.x & 31) == 0 && *(volatile int *)&h->flag) {
-        // after a timeout: wait (bounded) for the MMAs still in flight
-        const uint32_t e = tc_smem_addr(h->bar) + 16;
-        if (commits[0]) tc_mbar_wait(e, (commits[0] - 1) & 1, TC_WAIT_NS);
-        if (commits[1]) tc_mbar_wait(e + 8, (commits[1] - 1) & 1, TC_WAIT_NS);
+    if (*(volatile int *)&h->flag) {
+        // after a timeout: wait (bounded) for the MMAs and copies still in flight
+        if (mma_warp && (threadIdx.x & 31) == 0) {
+            const uint32_t e = tc_smem_addr(h->bar) + 16;
+            if (commits[0]) tc_mbar_wait(e, (commits[0] - 1) & 1, TC_WAIT_NS);
+            if (commits[1]) tc_mbar_wait(e + 8, (commits[1] - 1) & 1, TC_WAIT_NS);
+        }
+        if (copies && threadIdx.x == 0) {
+            const uint32_t c = tc_smem_addr(h->bar) + 40;
+            if (copies[0]) tc_mbar_wait(c, (copies[0] - 1) & 1, TC_WAIT_NS);
+            if (copies[1]) tc_mbar_wait(c + 8, (copies[1] - 1) & 1, TC_WAIT_NS);
+        }
     }
     tc_fence_before_sync();
     __syncthreads();
@@ -291,7 +305,7 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
         const int buf = s & 1, cs = s % TC_CHUNK_STAGES;
         const bool chunk_end = cs == TC_CHUNK_STAGES - 1 || s == nst - 1;
         if (mma_warp) {
-            if (lane == 0) tc_issue_stage<GR_LEVELS>(h, sbase, tmem, N, s, cs, commits, err);
+            if (lane == 0) tc_issue_stage<GR_LEVELS, false>(h, sbase, tmem, N, s, cs, commits, err);
             __syncwarp();
         } else {
             if (s >= 2 && !tc_mbar_wait(tc_smem_addr(h->bar) + 16 + 8 * buf, ((s >> 1) - 1) & 1, TC_WAIT_NS))
@@ -355,7 +369,7 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
             }
         }
     }
-    tc_release(h, tmem, mma_warp, commits);
+    tc_release(h, tmem, mma_warp, commits, nullptr);
 }
 
 // a[i + j*lda] = sum_r V[r,i] W[r,j] to FP64 accuracy on the tensor cores.
@@ -540,6 +554,7 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
 #pragma unroll
     for (int q = 0; q < TC_COLS_PER_WARP; ++q) acc[q] = 0.0;
     int commits[3] = {0, 0, 0};
+    int copies[2] = {0, 0};                              // bulk copies per buffer (thread 0)
 
     // split-warp geometry: core q = warp + 15 cc (A cores only); lane (r8, kp):
     // row 8g + r8, entries 8c + 2 kp and 8c + 2 kp + 1
@@ -563,13 +578,22 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
         const int buf = s & 1, cs = s % chunk_stages;
         const bool chunk_end = cs == chunk_stages - 1 || s == nst - 1;
         if (mma_warp) {
-            if (lane == 0) tc_issue_stage<LC_LEVELS>(h, sbase, tmem, N, s, cs, commits, err);
+            if (lane == 0) tc_issue_stage<LC_LEVELS, true>(h, sbase, tmem, N, s, cs, commits, err);
             __syncwarp();
         } else {
             if (s >= 2 && !tc_mbar_wait(tc_smem_addr(h->bar) + 16 + 8 * buf, ((s >> 1) - 1) & 1, TC_WAIT_NS))
                 tc_fail(h, err);
             uint8_t *A = sm + buf * TC_STAGE;
             uint8_t *B = A + OZ_DIGITS * TC_APLANE;
+            const uint32_t full = tc_smem_addr(h->bar) + 8 * buf;
+            // the pre-split C planes of this stage: one bulk copy, completing on copied[buf]
+            if (tid == 0) {
+                const uint32_t copied = tc_smem_addr(h->bar) + 40 + 8 * buf;
+                tc_mbar_arrive_expect_tx(copied, OZ_DIGITS * TC_BPLANE);
+                tc_bulk_g2s(tc_smem_addr(B), Bd + (size_t)(jt * nst + s) * (OZ_DIGITS * TC_BPLANE / 16),
+                            OZ_DIGITS * TC_BPLANE, copied);
+                ++copies[buf];
+            }
             const int ib = s * TC_KS + 2 * kp;
 #pragma unroll
             for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
@@ -586,13 +610,8 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
                     for (int p = 0; p < OZ_DIGITS; ++p) dst[p * (TC_APLANE / 4)] = oz_pack(u0, u1, p);
                 }
             }
-            {
-                const uint4 *src = Bd + (size_t)(jt * nst + s) * (OZ_DIGITS * TC_BPLANE / 16);
-                uint4 *dst = (uint4 *)B;
-                for (int v = tid; v < OZ_DIGITS * TC_BPLANE / 16; v += TC_SPLIT_THREADS) dst[v] = src[v];
-            }
             tc_fence_async_smem();
-            tc_mbar_arrive(tc_smem_addr(h->bar) + 8 * buf);
+            tc_mbar_arrive(full);
             if (s + 1 < nst) load_stage(s + 1);          // in flight while the MMAs run
         }
         if (chunk_end) {
@@ -643,7 +662,7 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
             }
         }
     }
-    tc_release(h, tmem, mma_warp, commits);
+    tc_release(h, tmem, mma_warp, commits, copies);
 }
 
 extern "C" int gb_lincomb_tc_ok(int k1) { return k1 <= LC_MAX_K; }

@@ -65,6 +65,20 @@ __device__ __forceinline__ void tc_mbar_arrive(uint32_t bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
+// arrival that also expects `bytes` of asynchronous copies to complete on the barrier
+__device__ __forceinline__ void tc_mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16),
+// completing its bytes on the mbarrier
+__device__ __forceinline__ void tc_bulk_g2s(uint32_t dst_smem, const void *src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     dst_smem),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
 // barrier over the first `count` threads of the CTA (named barrier `id`, 1..15)
 __device__ __forceinline__ void tc_bar_sync(int id, int count)
 {
