@@ -368,6 +368,47 @@ def run_reference(args, dist):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_kernel(args):
+    """One hot operation through the public binding (for per-kernel timing and ncu
+    captures): --warmup untimed calls, then --steps timed calls. spmm_a / spmm_b: the
+    FP64 product of the Q1 cube stiffness / mass (--ne elements per edge) with 64
+    columns; lincomb: Y = X C, X n x 178, C 178 x 64; gram: V^T W, V n x 178,
+    W n x 64 (--n rows)."""
+    import numpy as np
+    import gcge_gb300 as G
+    from gcge_gb300 import problems as P
+    ctx = G.Context(0)
+    rng = np.random.default_rng(0)
+    if args.kernel.startswith("spmm"):
+        A, B = P.fem_q1_cube(args.ne)
+        Msp = A if args.kernel == "spmm_a" else B
+        M, k, n = ctx.matrix(Msp), 64, A.n
+        X, Y = ctx.multivec(n, k, rng.standard_normal((n, k))), ctx.multivec(n, k)
+        op = lambda: G.mat_dot_multivec(M, X, Y, (0, 0), (k, k))
+        flops, desc = 2.0 * Msp.nnz * k, "n=%d nnz=%d k=%d" % (n, Msp.nnz, k)
+    else:
+        n, k1, k2 = args.n, 178, 64
+        X = ctx.multivec(n, k1, rng.standard_normal((n, k1)))
+        Y = ctx.multivec(n, k2, rng.standard_normal((n, k2)))
+        C = np.asfortranarray(rng.standard_normal((k1, k2))).ravel(order="F")
+        if args.kernel == "lincomb":
+            op = lambda: G.multivec_linear_comb(X, Y, (0, 0), (k1, k2), C, k1)
+        else:
+            op = lambda: G.multivec_inner_prod(X, Y, (0, 0), (k1, k2), k1)
+        flops, desc = 2.0 * n * k1 * k2, "n=%d k1=%d k2=%d" % (n, k1, k2)
+    for _ in range(args.warmup):
+        op()
+    ctx.sync()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        op()
+    ctx.sync()
+    dt = (time.perf_counter() - t) / max(args.steps, 1)
+    ctx.close()
+    print(json.dumps({"kernel": args.kernel, "shape": desc, "ms_per_call": dt * 1e3,
+                      "fp64_equiv_tflops": flops / dt / 1e12 if dt > 0 else None}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -380,7 +421,14 @@ def main():
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "lincomb", "gram"],
+                    help="time one hot operation instead of the solve (profiling)")
+    ap.add_argument("--n", type=int, default=262144, help="rows for --kernel lincomb/gram")
+    ap.add_argument("--ne", type=int, default=64, help="cube edge for --kernel spmm_a/spmm_b")
     args = ap.parse_args()
+    if args.kernel:
+        run_kernel(args)
+        return
     dist = Dist()
     out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
     if out is not None and dist.rank == 0:
