@@ -354,6 +354,7 @@ k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const 
 
 // W = A P (FP32, the first nact columns) and block partials of p.w: L lanes per
 // row, 4 columns per lane, 256 / L rows per block pass; grid-stride over rows
+// (measured faster than contiguous row ranges per block on the Q1 cube)
 template <int L>
 __global__ void __launch_bounds__(VB_THREADS)
 k_spmm32_dot(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,

@@ -420,6 +420,7 @@ extern "C" int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double
 #define LC_SMEM (2 * TC_STAGE + TC_HDR + 4 * LC_MAX_K)
 #define LC_OUT_LD (TC_N + 1)                         // doubles per staged output row
 #define LC_CORES_PER_WARP ((TC_ACORES + TC_SPLIT_WARPS - 1) / TC_SPLIT_WARPS)
+#define LC_SCALE_LOADS 48                            // row-scale loads in flight per thread
 // Levels 0-7 (34 digit pairs; 8 x 64 TMEM columns): the dropped pairs (level >= 8)
 // lie below 2^-55 of the scale product per term; level 7 (weight 2^-56) needs no
 // exactness, levels 0-6 stay exact for OZ_EXACT_TERMS terms.
@@ -513,33 +514,32 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
     for (int i = tid; i < k1; i += TC_THREADS) gs[i] = g_in[i];
     if (tid < TC_N) ecs[tid] = j0 + tid < k2 ? ec[j0 + tid] : OZ_NO_EXP;
     __syncthreads();
-    // row scales of X 2^g: warp w, rows w + 16 q (q < 8); 16 loads in flight
+    // row scales of X 2^g: 4 threads per row, up to LC_SCALE_LOADS independent loads
+    // of the high words (sign, exponent) in flight per thread before any is used
     {
-        int e[8];
+        const int rr = tid >> 2, t4 = tid & 3;
+        const long r = row0 + rr;
+        const bool rin = r < n;
+        const unsigned *xh = reinterpret_cast<const unsigned *>(X + (rin ? r : row0) * ldx) + 1;
+        int e = OZ_NO_EXP;
+        for (int i0 = t4; i0 < k1; i0 += 4 * LC_SCALE_LOADS) {
+            unsigned w[LC_SCALE_LOADS];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) e[q] = OZ_NO_EXP;
-        for (int i = lane; i < k1; i += 64) {
-            double xa[8], xb[8];
-            const int i2 = i + 32;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const long r = row0 + warp + 16 * q;
-                xa[q] = r < n ? X[r * ldx + i] : 0.0;
-                xb[q] = (r < n && i2 < k1) ? X[r * ldx + i2] : 0.0;
+            for (int j = 0; j < LC_SCALE_LOADS; ++j) {
+                const int i = i0 + 4 * j;
+                w[j] = (rin && i < k1) ? __ldg(xh + 2 * (long)i) : 0u;
             }
-            const int ga = gs[i], gb = i2 < k1 ? gs[i2] : OZ_NO_EXP;
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int ea = oz_exponent(xa[q]), eb = oz_exponent(xb[q]);
-                if (ea != OZ_NO_EXP && ga != OZ_NO_EXP) e[q] = max(e[q], ea + ga);
-                if (eb != OZ_NO_EXP && gb != OZ_NO_EXP) e[q] = max(e[q], eb + gb);
+            for (int j = 0; j < LC_SCALE_LOADS; ++j) {
+                const int i = i0 + 4 * j;
+                const int ex = (int)((w[j] >> 20) & 0x7ff);
+                const int gi = i < k1 ? gs[i] : OZ_NO_EXP;
+                if (ex && gi != OZ_NO_EXP) e = max(e, ex - 1022 + gi);
             }
         }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int m = __reduce_max_sync(0xffffffffu, e[q]);
-            if (lane == 0) er[warp + 16 * q] = m;
-        }
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
+        if (t4 == 0) er[rr] = e;
     }
     tc_fence_before_sync();
     __syncthreads();
