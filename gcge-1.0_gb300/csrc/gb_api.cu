@@ -619,10 +619,13 @@ extern "C" int gb_orth_ws_alloc(gcge_gpu_ctx *ctx, gb_orth_ws *ws, int n, int ma
     ws->max_start = max_start;
     ws->ld1 = (max_width + 1) & ~1;
     size_t kk = (size_t)max_width * max_width;
-    size_t sk = (size_t)(max_start > 0 ? max_start : 1) * max_width;
+    // Gram blocks up to [V W]^T (B W): (max_start + max_width) x max_width
+    size_t sk = ((size_t)(max_start > 0 ? max_start : 1) + max_width) * max_width;
+    ws->g_cap = kk > sk ? kk : sk;
     if (cudaMalloc(&ws->T1, sizeof(double) * (size_t)n * ws->ld1) != cudaSuccess ||
         cudaMalloc(&ws->G, sizeof(double) * (kk > sk ? kk : sk)) != cudaSuccess ||
         cudaMalloc(&ws->Tm, sizeof(double) * kk) != cudaSuccess ||
+        cudaMalloc(&ws->Cm, sizeof(double) * ((size_t)max_start + max_width) * max_width) != cudaSuccess ||
         cudaMalloc(&ws->chol_work, sizeof(double) * 2 * kk) != cudaSuccess ||
         cudaMalloc(&ws->small, sizeof(double) * 64) != cudaSuccess ||
         cudaMalloc(&ws->kept_dev, sizeof(int) * 4) != cudaSuccess) {
@@ -637,18 +640,20 @@ extern "C" void gb_orth_ws_free(gb_orth_ws *ws)
     if (ws->T1) cudaFree(ws->T1);
     if (ws->G) cudaFree(ws->G);
     if (ws->Tm) cudaFree(ws->Tm);
+    if (ws->Cm) cudaFree(ws->Cm);
     if (ws->chol_work) cudaFree(ws->chol_work);
     if (ws->small) cudaFree(ws->small);
     if (ws->kept_dev) cudaFree(ws->kept_dev);
     memset(ws, 0, sizeof(*ws));
 }
 
-// Cholesky-QR of W (k columns) in the B inner product, with deflation, twice.
+// Cholesky-QR of W (k columns) in the B inner product, with deflation: passes
+// first .. 1 of the two (relative deflation tolerance 1e-12, then 1e-14).
 static int cholqr2(gcge_gpu_ctx *ctx, int n, double *W, long ldw, int *k_io, const gcge_gpu_mat *B, double zero_tol,
-                   gb_orth_ws *ws)
+                   gb_orth_ws *ws, int first = 0)
 {
     int k = *k_io;
-    for (int pass = 0; pass < 2 && k > 0; ++pass) {
+    for (int pass = first; pass < 2 && k > 0; ++pass) {
         const double *BW = W;
         long ldbw = ldw;
         int st;
@@ -675,39 +680,90 @@ static int cholqr2(gcge_gpu_ctx *ctx, int n, double *W, long ldw, int *k_io, con
     return GCGE_GPU_OK;
 }
 
+// The first projection pass is W -= V (V^T B W). The second computes B W once
+// more and, in the same Gram call, both G2 = V^T B W and W^T B W (V and W are
+// contiguous columns of one block). When no third pass is needed, the first
+// Cholesky-QR Gram of W - V G2 follows without another B product:
+//   (W - V G2)^T B (W - V G2) = W^T B W - G2^T G2,   as V^T B V = I,
+// and the projection and R^-1 are applied together: W <- [V W] [[-G2 T], [T]].
+// The second Cholesky-QR pass forms its B product afresh (it exists to repair
+// the rounding of the first).
 extern "C" int gb_orthonormalize(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int *end,
                                  const gcge_gpu_mat *B, int max_reorth_time, double zero_tol, gb_orth_ws *ws)
 {
     int k = *end - start;
     if (k <= 0) return GCGE_GPU_OK;
-    if (k > ws->max_width || start > ws->max_start) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    if (k > ws->max_width || start > ws->max_start || ((size_t)start + k) * k > ws->g_cap)
+        return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     double *W = V + start;
     int st;
+    auto bprod = [&](const double **BW, long *ldbw) -> int {
+        *BW = W;
+        *ldbw = ldv;
+        if (!B) return GCGE_GPU_OK;
+        *BW = ws->T1;
+        *ldbw = ws->ld1;
+        return gb_spmm(ctx, B, W, ldv, ws->T1, ws->ld1, k, 1.0, nullptr, 0.0, nullptr);
+    };
     if (start > 0) {
         const int passes = max_reorth_time < 1 ? 1 : max_reorth_time;
-        double g1 = 0;
-        for (int pass = 0; pass < passes; ++pass) {
-            const double *BW = W;
-            long ldbw = ldv;
-            if (B) {
-                if ((st = gb_spmm(ctx, B, W, ldv, ws->T1, ws->ld1, k, 1.0, nullptr, 0.0, nullptr))) return st;
-                BW = ws->T1;
-                ldbw = ws->ld1;
-            }
-            if ((st = gb_gram(ctx, n, start, k, V, ldv, BW, ldbw, ws->G, start, 0))) return st;
-            if ((st = gb_lincomb(ctx, n, start, k, V, ldv, ws->G, start, -1.0, 1.0, W, ldv, 0))) return st;
-            // "twice is enough": a third pass only if the second still removed a sizeable part
-            if (pass == 0 && passes > 2) {
-                if ((st = gb_frobenius(ctx, start, k, ws->G, start, ws->small))) return st;
-            } else if (pass == 1 && passes > 2) {
-                if ((st = gb_frobenius(ctx, start, k, ws->G, start, ws->small + 1))) return st;
-                double h[2];
-                CUDA_TRY(ctx, cudaMemcpyAsync(h, ws->small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-                CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-                g1 = h[0];
-                if (!(h[1] > 1e-10 * g1)) break;
-            }
+        const double *BW;
+        long ldbw;
+        // projection pass 1
+        if ((st = bprod(&BW, &ldbw))) return st;
+        if ((st = gb_gram(ctx, n, start, k, V, ldv, BW, ldbw, ws->G, start, 0))) return st;
+        if ((st = gb_lincomb(ctx, n, start, k, V, ldv, ws->G, start, -1.0, 1.0, W, ldv, 0))) return st;
+        if (passes == 1) {
+            if ((st = cholqr2(ctx, n, W, ldv, &k, B, zero_tol, ws))) return st;
+            *end = start + k;
+            return GCGE_GPU_OK;
         }
+        if (passes > 2 && (st = gb_frobenius(ctx, start, k, ws->G, start, ws->small))) return st;
+        // projection pass 2: [V W]^T B W in one Gram (ld start + k)
+        const int ldg = start + k;
+        if ((st = bprod(&BW, &ldbw))) return st;
+        if ((st = gb_gram(ctx, n, ldg, k, V, ldv, BW, ldbw, ws->G, ldg, 0))) return st;
+        bool third = false;
+        if (passes > 2) {
+            // "twice is enough": a third pass only if the second still removed a sizeable part
+            if ((st = gb_frobenius(ctx, start, k, ws->G, ldg, ws->small + 1))) return st;
+            double h[2];
+            CUDA_TRY(ctx, cudaMemcpyAsync(h, ws->small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+            CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+            third = h[1] > 1e-10 * h[0];
+        }
+        if (third) {
+            if ((st = gb_lincomb(ctx, n, start, k, V, ldv, ws->G, ldg, -1.0, 1.0, W, ldv, 0))) return st;
+            for (int pass = 2; pass < passes; ++pass) {
+                if ((st = bprod(&BW, &ldbw))) return st;
+                if ((st = gb_gram(ctx, n, start, k, V, ldv, BW, ldbw, ws->G, start, 0))) return st;
+                if ((st = gb_lincomb(ctx, n, start, k, V, ldv, ws->G, start, -1.0, 1.0, W, ldv, 0))) return st;
+            }
+            if ((st = cholqr2(ctx, n, W, ldv, &k, B, zero_tol, ws))) return st;
+            *end = start + k;
+            return GCGE_GPU_OK;
+        }
+        // first Cholesky-QR on S = W^T B W - G2^T G2, recombination in one linear combination
+        double *S = ws->G + start;
+        if ((st = gb_small_gemm(ctx, 'T', 'N', k, k, start, -1.0, ws->G, ldg, ws->G, ldg, 1.0, S, ldg))) return st;
+        if ((st = gb_chol_deflate(ctx, k, S, ldg, ws->Tm, ws->kept_dev, zero_tol, 1e-12, ws->chol_work))) return st;
+        int kept = 0;
+        CUDA_TRY(ctx, cudaMemcpyAsync(&kept, ws->kept_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (kept <= 0) {
+            *end = start;
+            return GCGE_GPU_OK;
+        }
+        if ((st = gb_small_gemm(ctx, 'N', 'N', start, kept, k, -1.0, ws->G, ldg, ws->Tm, k, 0.0, ws->Cm, ldg)))
+            return st;
+        CUDA_TRY(ctx, cudaMemcpy2DAsync(ws->Cm + start, sizeof(double) * ldg, ws->Tm, sizeof(double) * k,
+                                        sizeof(double) * k, kept, cudaMemcpyDeviceToDevice, ctx->stream));
+        if ((st = gb_lincomb(ctx, n, ldg, kept, V, ldv, ws->Cm, ldg, 1.0, 0.0, ws->T1, ws->ld1, 0))) return st;
+        if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldv))) return st;
+        k = kept;
+        if ((st = cholqr2(ctx, n, W, ldv, &k, B, zero_tol, ws, 1))) return st;
+        *end = start + k;
+        return GCGE_GPU_OK;
     }
     if ((st = cholqr2(ctx, n, W, ldv, &k, B, zero_tol, ws))) return st;
     *end = start + k;

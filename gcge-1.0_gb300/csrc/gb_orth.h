@@ -13,10 +13,12 @@ extern "C" {
 
 typedef struct {
     int max_width, max_start;
+    size_t g_cap;    /* doubles in G */
     double *T1;      /* n x ld1 block: B*W and the re-combined columns */
     long ld1;
-    double *G;       /* Gram blocks: max(max_start, max_width) x max_width */
+    double *G;       /* Gram blocks: (max_start + max_width) x max_width */
     double *Tm;      /* max_width^2 coefficient matrix */
+    double *Cm;      /* (max_start + max_width) x max_width recombination coefficients */
     double *chol_work;
     double *small;   /* norms */
     int *kept_dev;
@@ -29,7 +31,8 @@ void gb_orth_ws_free(gb_orth_ws *ws);
  * V[:, 0:start) and itself: up to max_reorth_time block projection passes (a
  * third only when the second still removed more than 1e-10 of the first), then
  * Cholesky-QR twice with deflation; kept columns are packed at start, *end
- * shrinks by the number dropped. */
+ * shrinks by the number dropped. With two projection passes, the first
+ * Cholesky-QR reuses the second pass's B product (see gb_api.cu). */
 int gb_orthonormalize(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int *end,
                       const gcge_gpu_mat *B, int max_reorth_time, double zero_tol, gb_orth_ws *ws);
 
