@@ -370,7 +370,9 @@ k_tridiag(int m, const double *__restrict__ H, int ldh, double *__restrict__ Aw,
     }
 }
 
-// number of eigenvalues of the tridiagonal (d, e2 = e^2) smaller than x
+// number of eigenvalues of the tridiagonal (d, e2 = e^2) smaller than x (the
+// ratio form of the Sturm sequence with the pivmin guard; its count is monotone
+// in x under IEEE arithmetic, which the bisection relies on inside clusters)
 __device__ __forceinline__ int sturm_count(int m, const double *d, const double *e2, double x, double pivmin)
 {
     double q = d[0] - x;
@@ -636,7 +638,7 @@ extern "C" int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int 
     const int tthreads = m >= 512 ? 1024 : (m >= 128 ? 512 : 256);
     GB_PROF(ctx, GB_K_EIG, 8.0 * m * m, 4.0 / 3.0 * m * (double)m * m);
     GB_LAUNCH(ctx, k_tridiag, 1, tthreads, 2 * m * sizeof(double), m, H, ldh, Aw, d, e, tau);
-    const int warps_per_block = 8;
+    const int warps_per_block = 1;     // one eigenvalue per SM: the Sturm chains use the FP64 pipe
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
     GB_LAUNCH(ctx, k_bisect, (nev + warps_per_block - 1) / warps_per_block, 32 * warps_per_block,
               2 * m * sizeof(double), m, d, e, il, iu, eval, info_dev);
