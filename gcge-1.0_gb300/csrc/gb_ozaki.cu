@@ -417,7 +417,8 @@ extern "C" int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double
 
 // ---------------------------------------------------------------- linear combination (tcgen05)
 #define LC_MAX_K 4096                                // inner dimension handled by the tensor-core path
-#define LC_SMEM (2 * TC_STAGE + TC_HDR + 4 * LC_MAX_K)
+#define LC_HDR 2048                                  // tc_hdr, er, er_next, ecs
+#define LC_SMEM (2 * TC_STAGE + LC_HDR + 4 * LC_MAX_K)
 #define LC_OUT_LD (TC_N + 1)                         // doubles per staged output row
 #define LC_CORES_PER_WARP ((TC_ACORES + TC_SPLIT_WARPS - 1) / TC_SPLIT_WARPS)
 #define LC_SCALE_LOADS 48                            // row-scale loads in flight per thread
@@ -490,7 +491,14 @@ k_lc_coef_split(int k1, int k2, const double *__restrict__ C, int ldc, int upper
 }
 
 // Y[r, j0 + j] = alpha sum_i X[r, i] C[i, j0 + j] + beta Y[r, j0 + j];
-// grid (ceil(n / 128), column tiles), TC_THREADS threads, LC_SMEM dynamic shared memory.
+// grid (P, column tiles) with P <= number of SMs, TC_THREADS threads, LC_SMEM
+// dynamic shared memory. Persistent: CTA b walks the 128-row tiles b, b + P, ...
+// with one TMEM allocation and one barrier set; the stage counter runs across
+// tiles. While the K stages of a tile run, the split warps also load the next
+// tile's entries of the same stage and fold their exponents into that tile's row
+// scales (shared-memory atomicMax), so only the first tile has a separate scale
+// pass and every later tile's X is already in L2 when it is split. The drain
+// writes Y directly.
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, const uint4 *__restrict__ Bd,
              const int *__restrict__ g_in, const int *__restrict__ ec, double alpha, double beta,
@@ -500,27 +508,29 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
     uint8_t *sm = tc_smem;
     if (*(volatile int *)err) return;                    // an earlier launch timed out: do nothing
     tc_hdr *h = (tc_hdr *)(sm + 2 * TC_STAGE);
-    int *er = (int *)(sm + 2 * TC_STAGE + 64);           // [TC_M] row scales of X 2^g
-    int *ecs = er + TC_M;                                // [TC_N] column scales of 2^-g C
-    int *gs = (int *)(sm + 2 * TC_STAGE + TC_HDR);       // [k1] inner-dimension scales g
+    int *er = (int *)(sm + 2 * TC_STAGE + 64);           // [TC_M] row scales of X 2^g, this tile
+    int *er_next = er + TC_M;                            // [TC_M] the same for the next tile
+    int *ecs = er_next + TC_M;                           // [TC_N] column scales of 2^-g C
+    int *gs = (int *)(sm + 2 * TC_STAGE + LC_HDR);       // [k1] inner-dimension scales g
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long row0 = (long)blockIdx.x * TC_M;
     const int jt = blockIdx.y, j0 = jt * TC_N;
     const int N = min(TC_N, (k2 - j0 + 15) & ~15);
+    const long ntiles = ((long)n + TC_M - 1) / TC_M;
     // one exact accumulation over all of K when it is short enough
     const int chunk_stages = k1 <= OZ_EXACT_TERMS ? nst : TC_CHUNK_STAGES;
 
     tc_setup(h);
     for (int i = tid; i < k1; i += TC_THREADS) gs[i] = g_in[i];
     if (tid < TC_N) ecs[tid] = j0 + tid < k2 ? ec[j0 + tid] : OZ_NO_EXP;
+    if (tid < TC_M) er_next[tid] = OZ_NO_EXP;
     __syncthreads();
-    // row scales of X 2^g: 4 threads per row, up to LC_SCALE_LOADS independent loads
-    // of the high words (sign, exponent) in flight per thread before any is used
+    // row scales of the first tile: 4 threads per row, up to LC_SCALE_LOADS
+    // independent loads of the high words (sign, exponent) in flight per thread
     {
         const int rr = tid >> 2, t4 = tid & 3;
-        const long r = row0 + rr;
+        const long r = (long)blockIdx.x * TC_M + rr;
         const bool rin = r < n;
-        const unsigned *xh = reinterpret_cast<const unsigned *>(X + (rin ? r : row0) * ldx) + 1;
+        const unsigned *xh = reinterpret_cast<const unsigned *>(X + (rin ? r : 0) * ldx) + 1;
         int e = OZ_NO_EXP;
         for (int i0 = t4; i0 < k1; i0 += 4 * LC_SCALE_LOADS) {
             unsigned w[LC_SCALE_LOADS];
@@ -549,10 +559,7 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
     const int quarter = warp & 3, col0 = (warp >> 2) * TC_COLS_PER_WARP;
     const int my_row = quarter * 32 + lane;
     const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + col0;
-    const int my_e = er[my_row];
-    double acc[TC_COLS_PER_WARP];
-#pragma unroll
-    for (int q = 0; q < TC_COLS_PER_WARP; ++q) acc[q] = 0.0;
+    const bool plain = beta == 0.0 && (alpha == 1.0 || alpha == -1.0);
     int commits[3] = {0, 0, 0};
     int copies[2] = {0, 0};                              // bulk copies per buffer (thread 0)
 
@@ -560,7 +567,7 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
     // row 8g + r8, entries 8c + 2 kp and 8c + 2 kp + 1
     const int r8 = lane >> 2, kp = lane & 3;
     double xv[LC_CORES_PER_WARP][2];
-    auto load_stage = [&](int s) {
+    auto load_stage = [&](long row0, int s) {
         const int ib = s * TC_KS + 2 * kp;
 #pragma unroll
         for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
@@ -572,95 +579,139 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
             xv[cc][1] = (in && i + 1 < k1) ? X[r * ldx + i + 1] : 0.0;
         }
     };
-    if (!mma_warp) load_stage(0);
+    if (!mma_warp) load_stage((long)blockIdx.x * TC_M, 0);
 
-    for (int s = 0; s < nst; ++s) {
-        const int buf = s & 1, cs = s % chunk_stages;
-        const bool chunk_end = cs == chunk_stages - 1 || s == nst - 1;
-        if (mma_warp) {
-            if (lane == 0) tc_issue_stage<LC_LEVELS, true>(h, sbase, tmem, N, s, cs, commits, err);
-            __syncwarp();
-        } else {
-            if (s >= 2 && !tc_mbar_wait(tc_smem_addr(h->bar) + 16 + 8 * buf, ((s >> 1) - 1) & 1, TC_WAIT_NS))
-                tc_fail(h, err);
-            uint8_t *A = sm + buf * TC_STAGE;
-            uint8_t *B = A + OZ_DIGITS * TC_APLANE;
-            const uint32_t full = tc_smem_addr(h->bar) + 8 * buf;
-            // the pre-split C planes of this stage: one bulk copy, completing on copied[buf]
-            if (tid == 0) {
-                const uint32_t copied = tc_smem_addr(h->bar) + 40 + 8 * buf;
-                tc_mbar_arrive_expect_tx(copied, OZ_DIGITS * TC_BPLANE);
-                tc_bulk_g2s(tc_smem_addr(B), Bd + (size_t)(jt * nst + s) * (OZ_DIGITS * TC_BPLANE / 16),
-                            OZ_DIGITS * TC_BPLANE, copied);
-                ++copies[buf];
-            }
-            const int ib = s * TC_KS + 2 * kp;
+    int gsc = 0;                                         // stages issued by this CTA, over all tiles
+    bool stop = false;
+    for (long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+        const long row0 = t * TC_M, nrow0 = row0 + (long)gridDim.x * TC_M;
+        const bool has_next = t + gridDim.x < ntiles;
+        const int my_e = er[my_row];
+        double acc[TC_COLS_PER_WARP];
 #pragma unroll
-            for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
-                const int q = warp + TC_SPLIT_WARPS * cc;
-                if (q < TC_ACORES) {
-                    const int i = ib + 8 * (q & 3);
-                    const int e = er[8 * (q >> 2) + r8];
-                    // a zero row of C (g = OZ_NO_EXP) contributes nothing: its digits stay zero
-                    const int g0 = i < k1 ? gs[i] : OZ_NO_EXP, g1 = i + 1 < k1 ? gs[i + 1] : OZ_NO_EXP;
-                    const unsigned long long u0 = g0 != OZ_NO_EXP ? oz_bias(xv[cc][0], e - g0) : OZ_BIAS;
-                    const unsigned long long u1 = g1 != OZ_NO_EXP ? oz_bias(xv[cc][1], e - g1) : OZ_BIAS;
-                    uint32_t *dst = (uint32_t *)(A + q * 128 + r8 * 16 + kp * 4);
-#pragma unroll
-                    for (int p = 0; p < OZ_DIGITS; ++p) dst[p * (TC_APLANE / 4)] = oz_pack(u0, u1, p);
+        for (int q = 0; q < TC_COLS_PER_WARP; ++q) acc[q] = 0.0;
+        for (int s = 0; s < nst; ++s, ++gsc) {
+            const int buf = gsc & 1, cs = s % chunk_stages;
+            const bool chunk_end = cs == chunk_stages - 1 || s == nst - 1;
+            if (mma_warp) {
+                if (lane == 0) tc_issue_stage<LC_LEVELS, true>(h, sbase, tmem, N, gsc, cs, commits, err);
+                __syncwarp();
+            } else {
+                if (gsc >= 2 && !tc_mbar_wait(tc_smem_addr(h->bar) + 16 + 8 * buf, ((gsc >> 1) - 1) & 1,
+                                              TC_WAIT_NS))
+                    tc_fail(h, err);
+                uint8_t *A = sm + buf * TC_STAGE;
+                uint8_t *B = A + OZ_DIGITS * TC_APLANE;
+                const uint32_t full = tc_smem_addr(h->bar) + 8 * buf;
+                // the pre-split C planes of this stage: one bulk copy, completing on copied[buf]
+                if (tid == 0) {
+                    const uint32_t copied = tc_smem_addr(h->bar) + 40 + 8 * buf;
+                    tc_mbar_arrive_expect_tx(copied, OZ_DIGITS * TC_BPLANE);
+                    tc_bulk_g2s(tc_smem_addr(B), Bd + (size_t)(jt * nst + s) * (OZ_DIGITS * TC_BPLANE / 16),
+                                OZ_DIGITS * TC_BPLANE, copied);
+                    ++copies[buf];
                 }
-            }
-            tc_fence_async_smem();
-            tc_mbar_arrive(full);
-            if (s + 1 < nst) load_stage(s + 1);          // in flight while the MMAs run
-        }
-        if (chunk_end) {
-            if (!tc_wait_chunk(h, s, err)) break;
-            const bool first = s < chunk_stages;
+                const int ib = s * TC_KS + 2 * kp;
 #pragma unroll
-            for (int g4 = 0; g4 < TC_COLS_PER_WARP / 4; ++g4) {
-                if (col0 + g4 * 4 < N) {
-                    uint32_t v[LC_LEVELS][4];
-                    tc_load_levels4<LC_LEVELS>(trow + g4 * 4, v);
+                for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
+                    const int q = warp + TC_SPLIT_WARPS * cc;
+                    if (q < TC_ACORES) {
+                        const int i = ib + 8 * (q & 3);
+                        const int e = er[8 * (q >> 2) + r8];
+                        // a zero row of C (g = OZ_NO_EXP) contributes nothing: its digits stay zero
+                        const int g0 = i < k1 ? gs[i] : OZ_NO_EXP, g1 = i + 1 < k1 ? gs[i + 1] : OZ_NO_EXP;
+                        const unsigned long long u0 = g0 != OZ_NO_EXP ? oz_bias(xv[cc][0], e - g0) : OZ_BIAS;
+                        const unsigned long long u1 = g1 != OZ_NO_EXP ? oz_bias(xv[cc][1], e - g1) : OZ_BIAS;
+                        uint32_t *dst = (uint32_t *)(A + q * 128 + r8 * 16 + kp * 4);
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        float lev[LC_LEVELS];
+                        for (int p = 0; p < OZ_DIGITS; ++p) dst[p * (TC_APLANE / 4)] = oz_pack(u0, u1, p);
+                    }
+                }
+                tc_fence_async_smem();
+                tc_mbar_arrive(full);
+                // in flight while the MMAs run: the next stage's values (or the next
+                // tile's first stage), and the next tile's entries of this stage for its scales
+                if (s + 1 < nst) load_stage(row0, s + 1);
+                else if (has_next) load_stage(nrow0, 0);
+                if (has_next) {
+                    unsigned w[LC_CORES_PER_WARP][2];
 #pragma unroll
-                        for (int L = 0; L < LC_LEVELS; ++L) lev[L] = __uint_as_float(v[L][q]);
-                        long long a, b;
-                        oz_levels_to_int<LC_LEVELS>(lev, a, b);
-                        const double d =
-                            oz_to_double<40>(a, b, my_e + ecs[col0 + g4 * 4 + q] - OZ_SCALE_OFFSET);
-                        acc[g4 * 4 + q] = first ? d : acc[g4 * 4 + q] + d;
+                    for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
+                        const int q = warp + TC_SPLIT_WARPS * cc;
+                        const long r = nrow0 + 8 * (q >> 2) + r8;
+                        const int i = ib + 8 * (q & 3);
+                        const bool in = q < TC_ACORES && r < n;
+                        const unsigned *xh = reinterpret_cast<const unsigned *>(X + (in ? r : 0) * ldx + i) + 1;
+                        w[cc][0] = (in && i < k1) ? __ldg(xh) : 0u;
+                        w[cc][1] = (in && i + 1 < k1) ? __ldg(xh + 2) : 0u;
+                    }
+#pragma unroll
+                    for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
+                        const int q = warp + TC_SPLIT_WARPS * cc;
+                        if (q < TC_ACORES) {
+                            const int i = ib + 8 * (q & 3);
+                            int e = OZ_NO_EXP;
+#pragma unroll
+                            for (int u = 0; u < 2; ++u) {
+                                const int ex = (int)((w[cc][u] >> 20) & 0x7ff);
+                                const int gi = i + u < k1 ? gs[i + u] : OZ_NO_EXP;
+                                if (ex && gi != OZ_NO_EXP) e = max(e, ex - 1022 + gi);
+                            }
+                            e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
+                            e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
+                            if (kp == 0 && e > OZ_NO_EXP) atomicMax(er_next + 8 * (q >> 2) + r8, e);
+                        }
                     }
                 }
             }
-            tc_fence_before_sync();
-            tc_mbar_arrive(tc_smem_addr(h->bar) + 32);
-            ++commits[2];
-        }
-        if (*(volatile int *)&h->flag) break;
-    }
-
-    __syncthreads();
-    if (!*(volatile int *)&h->flag) {
-        // stage the 128 x N block in shared memory (every MMA is done, the operand
-        // buffers are idle), then write Y row by row, coalesced
-        double *O = (double *)sm;
+            if (chunk_end) {
+                if (!tc_wait_chunk(h, gsc, err)) {
+                    stop = true;
+                    break;
+                }
+                const bool first = s < chunk_stages, last = s == nst - 1;
+                const long r = row0 + my_row;
 #pragma unroll
-        for (int q = 0; q < TC_COLS_PER_WARP; ++q) O[my_row * LC_OUT_LD + col0 + q] = acc[q];
-        __syncthreads();
-        const int ncol = min(TC_N, k2 - j0);
-        const bool plain = beta == 0.0 && (alpha == 1.0 || alpha == -1.0);
-        for (int rr = warp; rr < TC_M; rr += TC_WARPS) {
-            const long r = row0 + rr;
-            if (r >= n) break;
-            for (int q = lane; q < ncol; q += 32) {
-                double *y = Y + r * ldy + j0 + q;
-                const double v = O[rr * LC_OUT_LD + q];
-                *y = plain ? (alpha == 1.0 ? v : -v) : fma(beta, *y, alpha * v);
+                for (int g4 = 0; g4 < TC_COLS_PER_WARP / 4; ++g4) {
+                    if (col0 + g4 * 4 < N) {
+                        uint32_t v[LC_LEVELS][4];
+                        tc_load_levels4<LC_LEVELS>(trow + g4 * 4, v);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            float lev[LC_LEVELS];
+#pragma unroll
+                            for (int L = 0; L < LC_LEVELS; ++L) lev[L] = __uint_as_float(v[L][q]);
+                            long long a, b;
+                            oz_levels_to_int<LC_LEVELS>(lev, a, b);
+                            const double d =
+                                oz_to_double<40>(a, b, my_e + ecs[col0 + g4 * 4 + q] - OZ_SCALE_OFFSET);
+                            acc[g4 * 4 + q] = first ? d : acc[g4 * 4 + q] + d;
+                            const int j = j0 + col0 + g4 * 4 + q;
+                            if (last && r < n && j < k2) {
+                                double *y = Y + r * ldy + j;
+                                const double v2 = acc[g4 * 4 + q];
+                                *y = plain ? (alpha == 1.0 ? v2 : -v2) : fma(beta, *y, alpha * v2);
+                            }
+                        }
+                    }
+                }
+                tc_fence_before_sync();
+                tc_mbar_arrive(tc_smem_addr(h->bar) + 32);
+                ++commits[2];
+            }
+            if (*(volatile int *)&h->flag) {
+                stop = true;
+                break;
             }
         }
+        // tile end: every scale atomic of the next tile is done; er <- er_next
+        __syncthreads();
+        if (tid < TC_M) {
+            er[tid] = er_next[tid];
+            er_next[tid] = OZ_NO_EXP;
+        }
+        __syncthreads();
+        if (*(volatile int *)&h->flag) stop = true;
     }
     tc_release(h, tmem, mma_warp, commits, copies);
 }
@@ -688,7 +739,11 @@ extern "C" int gb_lincomb_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const dou
     GB_LAUNCH(ctx, k_lc_coef_split, dim3(nst, jtiles), 256, 0, k1, k2, C, ldc, upper, nst, g, ec, Bd);
     GB_PROF(ctx, GB_K_LINCOMB, 8.0 * n * k1 + (beta != 0.0 ? 16.0 : 8.0) * n * k2,
             upper ? 1.0 * n * k1 * (k2 + 1) : 2.0 * n * k1 * k2);
-    GB_LAUNCH(ctx, k_lincomb_tc, dim3((unsigned)((n + TC_M - 1) / TC_M), jtiles), TC_THREADS, LC_SMEM, n, k1, k2, X,
-              ldx, (const uint4 *)Bd, g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err);
+    const long ntiles = ((long)n + TC_M - 1) / TC_M;
+    long P = ctx->num_sms / jtiles;
+    if (P < 1) P = 1;
+    if (P > ntiles) P = ntiles;
+    GB_LAUNCH(ctx, k_lincomb_tc, dim3((unsigned)P, jtiles), TC_THREADS, LC_SMEM, n, k1, k2, X, ldx, (const uint4 *)Bd,
+              g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err);
     return GCGE_GPU_OK;
 }
