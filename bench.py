@@ -371,8 +371,8 @@ def run_reference(args, dist):
 def run_kernel(args):
     """One hot operation through the public binding (for per-kernel timing and ncu
     captures): --warmup untimed calls, then --steps timed calls. spmm_a / spmm_b: the
-    FP64 product of the Q1 cube stiffness / mass (--ne elements per edge) with 64
-    columns; lincomb: Y = X C, X n x 178, C 178 x 64; gram: V^T W, V n x 178,
+    FP64 product of the Q1 cube stiffness / mass (--ne elements per edge) with --k
+    columns (default 64); lincomb: Y = X C, X n x 178, C 178 x 64; gram: V^T W, V n x 178,
     W n x 64 (--n rows)."""
     import numpy as np
     import gcge_gb300 as G
@@ -382,7 +382,7 @@ def run_kernel(args):
     if args.kernel.startswith("spmm"):
         A, B = P.fem_q1_cube(args.ne)
         Msp = A if args.kernel == "spmm_a" else B
-        M, k, n = ctx.matrix(Msp), 64, A.n
+        M, k, n = ctx.matrix(Msp), args.k, A.n
         X, Y = ctx.multivec(n, k, rng.standard_normal((n, k))), ctx.multivec(n, k)
         op = lambda: G.mat_dot_multivec(M, X, Y, (0, 0), (k, k))
         flops, desc = 2.0 * Msp.nnz * k, "n=%d nnz=%d k=%d" % (n, Msp.nnz, k)
@@ -425,6 +425,7 @@ def main():
                     help="time one hot operation instead of the solve (profiling)")
     ap.add_argument("--n", type=int, default=262144, help="rows for --kernel lincomb/gram")
     ap.add_argument("--ne", type=int, default=64, help="cube edge for --kernel spmm_a/spmm_b")
+    ap.add_argument("--k", type=int, default=64, help="columns for --kernel spmm_a/spmm_b")
     args = ap.parse_args()
     if args.kernel:
         run_kernel(args)

@@ -83,12 +83,13 @@ k_spmm(int n, const int *__restrict__ rp, const int *__restrict__ ci, const VT *
 // 16 / sizeof(T) consecutive columns per lane, so each nonzero gathers its block
 // row of X with one 16-byte load per lane; 32 / L rows per warp. The group loads
 // up to L (column, value) pairs at once and broadcasts them with group-masked
-// shuffles. Needs X, Y and their leading dimensions 16-byte aligned.
+// shuffles. AL: X and ldx 16-byte aligned (otherwise the slice is read element
+// by element, for column ranges that start at an odd column).
 template <typename T> struct vec16;
 template <> struct vec16<float> { typedef float4 type; };
 template <> struct vec16<double> { typedef double2 type; };
 
-template <typename T, int L>
+template <typename T, int L, bool AL = true>
 __global__ void __launch_bounds__(256)
 k_spmm_vec(int n, const int *__restrict__ rp, const int *__restrict__ ci, const T *__restrict__ val,
            const T *__restrict__ X, long ldx, T *__restrict__ Y, long ldy, int k, T alpha,
@@ -124,10 +125,17 @@ k_spmm_vec(int n, const int *__restrict__ rp, const int *__restrict__ ci, const 
                 const T aa = __shfl_sync(gmask, a, t, L);
                 const T *xr = X + (long)jj * ldx + c;
                 if (full) {
-                    const V xv = __ldg(reinterpret_cast<const V *>(xr));
-                    const T *xs = reinterpret_cast<const T *>(&xv);
+                    if (AL) {
+                        const V xv = __ldg(reinterpret_cast<const V *>(xr));
+                        const T *xs = reinterpret_cast<const T *>(&xv);
 #pragma unroll
-                    for (int q = 0; q < VW; ++q) acc[q] = fma(aa, xs[q], acc[q]);
+                        for (int q = 0; q < VW; ++q) acc[q] = fma(aa, xs[q], acc[q]);
+                    } else {
+                        // X not 16-byte aligned (a column range starting at an odd
+                        // column): the same slice as VW element loads
+#pragma unroll
+                        for (int q = 0; q < VW; ++q) acc[q] = fma(aa, __ldg(xr + q), acc[q]);
+                    }
                 } else if (c < kact) {
                     // ragged tail (k not a multiple of VW); lanes past the last column
                     // skip both branches so the warp issues the vector FMAs only once
@@ -181,6 +189,102 @@ k_spmv(int n, const int *__restrict__ rp, const int *__restrict__ ci, const VT *
     }
 }
 
+// FP64 SpMM with a lane shape fitted to k: a group of L lanes (L = 4, 8, 16) owns
+// a row and every lane VW consecutive columns (VW = 1..8, element loads), so
+// that L VW covers k with few idle lanes -- the FP64 pipe spends its issue slots
+// on idle lanes too, and k (the unconverged columns) shrinks during a solve.
+// 32 / L rows per warp; (column, value) pairs broadcast by group shuffles. Every
+// lane runs the same instruction stream: a lane whose columns run past k reads
+// the window [k - VW, k) instead (VW <= k, so it stays inside the range) and
+// stores only the columns it owns, so that no lane diverges in the inner loop.
+template <int L, int VW>
+__global__ void __launch_bounds__(256)
+k_spmm64_lv(int n, const int *__restrict__ rp, const int *__restrict__ ci, const double *__restrict__ val,
+            const double *__restrict__ X, long ldx, double *__restrict__ Y, long ldy, int k, double alpha,
+            const double *__restrict__ alpha_col, double beta, const int *__restrict__ ncols_dev)
+{
+    constexpr int RPW = 32 / L;
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / L, sl = lane % L;
+    const unsigned gmask = (L == 32) ? FULL : (((1u << L) - 1u) << (sub * L));
+    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long row = warp * RPW + sub;
+    int kact = k;
+    if (ncols_dev) kact = min(k, *ncols_dev);
+    if (row >= n || kact <= 0) return;                    // uniform within the row group
+    const int beg = rp[row], end = rp[row + 1];
+    for (int c0 = 0; c0 < kact; c0 += L * VW) {
+        const int c = c0 + sl * VW;                       // first column this lane owns
+        const int cb = min(c, k - VW);                    // first column it reads
+        double acc[VW];
+#pragma unroll
+        for (int q = 0; q < VW; ++q) acc[q] = 0;
+        for (int base = beg; base < end; base += L) {
+            const int e = base + sl;
+            int j = 0;
+            double a = 0;
+            if (e < end) { j = __ldg(ci + e); a = __ldg(val + e); }
+            const int cnt = min(L, end - base);
+#pragma unroll 4
+            for (int t = 0; t < cnt; ++t) {
+                const int jj = __shfl_sync(gmask, j, t, L);
+                const double aa = __shfl_sync(gmask, a, t, L);
+                const double *xr = X + (long)jj * ldx + cb;
+#pragma unroll
+                for (int q = 0; q < VW; ++q) acc[q] = fma(aa, __ldg(xr + q), acc[q]);
+            }
+        }
+        double *yr = Y + row * ldy + cb;
+#pragma unroll
+        for (int q = 0; q < VW; ++q) {
+            const int col = cb + q;
+            if (col < c || col >= kact) continue;
+            const double s = alpha * (alpha_col ? alpha_col[col] : 1.0);
+            yr[q] = beta == 0.0 ? s * acc[q] : s * acc[q] + beta * yr[q];
+        }
+    }
+}
+
+// (L, VW) with the fewest idle lane slots for k columns (ties: the larger L)
+static void spmm64_shape(int k, int *Lo, int *VWo)
+{
+    double best = -1;
+    for (int L = 16; L >= 4; L >>= 1) {
+        int vw = (k + L - 1) / L;
+        if (vw > 8) vw = 8;
+        const int cols = L * vw, chunks = (k + cols - 1) / cols;
+        const double eff = (double)k / ((double)chunks * cols);
+        if (eff > best + 1e-12) {
+            best = eff;
+            *Lo = L;
+            *VWo = vw;
+        }
+    }
+}
+
+#define SPMM64_CASE(LL, VV)                                                                               \
+    if (L == LL && VW == VV) {                                                                            \
+        GB_LAUNCH(ctx, (k_spmm64_lv<LL, VV>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k, alpha, \
+                  alpha_col, beta, ncols_dev);                                                            \
+        return GCGE_GPU_OK;                                                                               \
+    }
+#define SPMM64_L(LL) SPMM64_CASE(LL, 1) SPMM64_CASE(LL, 2) SPMM64_CASE(LL, 3) SPMM64_CASE(LL, 4) \
+    SPMM64_CASE(LL, 5) SPMM64_CASE(LL, 6) SPMM64_CASE(LL, 7) SPMM64_CASE(LL, 8)
+
+static int spmm64_lv_launch(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X, long ldx, double *Y,
+                            long ldy, int k, double alpha, const double *alpha_col, double beta,
+                            const int *ncols_dev)
+{
+    int L = 16, VW = 4;
+    spmm64_shape(k, &L, &VW);
+    const long warps = ((long)A->n * L + 31) / 32;
+    const int grid = ceil_div_l(warps * 32, 256);
+    SPMM64_L(4)
+    SPMM64_L(8)
+    SPMM64_L(16)
+    return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+}
+
 extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X, long ldx, double *Y,
                        long ldy, int k, double alpha, const double *alpha_col, double beta,
                        const int *ncols_dev)
@@ -193,31 +297,9 @@ extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X
         int grid = ceil_div_l((long)A->n * 32, 256);
         GB_LAUNCH(ctx, (k_spmv<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
                   Y, ldy, alpha, alpha_col, beta, ncols_dev);
-    } else {
-        if (aligned16(X, ldx, sizeof(double)) && aligned16(Y, ldy, sizeof(double))) {
-            const int L = spmm_vec_lanes<double>(k);
-            const long warps = ((long)A->n * L + 31) / 32;
-            const int grid = ceil_div_l(warps * 32, 256);
-            if (L == 4)
-                GB_LAUNCH(ctx, (k_spmm_vec<double, 4>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
-                          alpha, alpha_col, beta, ncols_dev);
-            else if (L == 8)
-                GB_LAUNCH(ctx, (k_spmm_vec<double, 8>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
-                          alpha, alpha_col, beta, ncols_dev);
-            else if (L == 16)
-                GB_LAUNCH(ctx, (k_spmm_vec<double, 16>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
-                          alpha, alpha_col, beta, ncols_dev);
-            else
-                GB_LAUNCH(ctx, (k_spmm_vec<double, 32>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, k,
-                          alpha, alpha_col, beta, ncols_dev);
-        } else {
-            long warps = (long)A->n * ((k + 63) / 64);
-            int grid = ceil_div_l(warps * 32, 256);
-            GB_LAUNCH(ctx, (k_spmm<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
-                      Y, ldy, k, alpha, alpha_col, beta, ncols_dev);
-        }
+        return GCGE_GPU_OK;
     }
-    return GCGE_GPU_OK;
+    return spmm64_lv_launch(ctx, A, X, ldx, Y, ldy, k, alpha, alpha_col, beta, ncols_dev);
 }
 
 extern "C" int gb_spmm32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const float *X, long ldx, float *Y,

@@ -39,16 +39,17 @@ def cols_to_oracle(X):
 @pytest.mark.parametrize("maker,k", [(lambda: P.laplace2d(37, 23)[0], 1), (lambda: P.laplace2d(37, 23)[0], 7),
                                      (lambda: P.fem_q1_cube(9)[0], 64), (lambda: P.fem_q1_cube(9)[1], 65),
                                      (lambda: P.powerlaw_graph(3000, seed=5, dmax=300)[0], 33)])
-def test_matdotmultivec(ctx, oracle, maker, k):
+@pytest.mark.parametrize("sx,sy", [(2, 4), (1, 3)])      # (1, 3): column ranges off the 16-byte grid
+def test_matdotmultivec(ctx, oracle, maker, k, sx, sy):
     A = maker()
     rng = np.random.default_rng(1)
     X = rng.standard_normal((A.n, k + 3))
     dA = ctx.matrix(A)
     x = ctx.multivec(A.n, k + 3, X)
     y = ctx.multivec(A.n, k + 5)
-    G.mat_dot_multivec(dA, x, y, (2, 4), (2 + k, 4 + k))
-    got = y.download()[:, 4:4 + k]
-    ref = oracle.matmultivec(A, cols_to_oracle(X[:, 2:2 + k])).T
+    G.mat_dot_multivec(dA, x, y, (sx, sy), (sx + k, sy + k))
+    got = y.download()[:, sy:sy + k]
+    ref = oracle.matmultivec(A, cols_to_oracle(X[:, sx:sx + k])).T
     assert rel(got, ref) < RTOL
 
 
