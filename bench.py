@@ -372,7 +372,8 @@ def run_kernel(args):
     """One hot operation through the public binding (for per-kernel timing and ncu
     captures): --warmup untimed calls, then --steps timed calls. spmm_a / spmm_b: the
     FP64 product of the Q1 cube stiffness / mass (--ne elements per edge) with --k
-    columns (default 64); lincomb: Y = X C, X n x 178, C 178 x 64; gram: V^T W, V n x 178,
+    columns (default 64); bcg32: one mixed-precision block CG call on the stiffness
+    with --k columns and 20 FP32 rounds (every column kept active); lincomb: Y = X C, X n x 178, C 178 x 64; gram: V^T W, V n x 178,
     W n x 64 (--n rows)."""
     import numpy as np
     import gcge_gb300 as G
@@ -386,6 +387,13 @@ def run_kernel(args):
         X, Y = ctx.multivec(n, k, rng.standard_normal((n, k))), ctx.multivec(n, k)
         op = lambda: G.mat_dot_multivec(M, X, Y, (0, 0), (k, k))
         flops, desc = 2.0 * Msp.nnz * k, "n=%d nnz=%d k=%d" % (n, Msp.nnz, k)
+    elif args.kernel == "bcg32":
+        A, _ = P.fem_q1_cube(args.ne)
+        M, k, n = ctx.matrix(A, keep_fp32=True), args.k, A.n
+        R = ctx.multivec(n, k, rng.standard_normal((n, k)))
+        W = ctx.multivec(n, k)
+        op = lambda: G.bcg(M, R, 0, W, 0, k, cg_max_it=20, cg_rate=1e-30, precision=1)
+        flops, desc = 2.0 * 20 * A.nnz * k, "n=%d nnz=%d k=%d rounds=20" % (n, A.nnz, k)
     else:
         n, k1, k2 = args.n, 178, 64
         X = ctx.multivec(n, k1, rng.standard_normal((n, k1)))
@@ -421,11 +429,11 @@ def main():
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "lincomb", "gram"],
+    ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "bcg32", "lincomb", "gram"],
                     help="time one hot operation instead of the solve (profiling)")
     ap.add_argument("--n", type=int, default=262144, help="rows for --kernel lincomb/gram")
     ap.add_argument("--ne", type=int, default=64, help="cube edge for --kernel spmm_a/spmm_b")
-    ap.add_argument("--k", type=int, default=64, help="columns for --kernel spmm_a/spmm_b")
+    ap.add_argument("--k", type=int, default=64, help="columns for --kernel spmm_a/spmm_b/bcg32")
     args = ap.parse_args()
     if args.kernel:
         run_kernel(args)

@@ -215,14 +215,6 @@ static int row_grid(gcge_gpu_ctx *ctx, long rows)
     return (int)g;
 }
 
-static int elem_grid(gcge_gpu_ctx *ctx, long total)
-{
-    long g = (total + 255) / 256, cap = (long)ctx->num_sms * 16;
-    if (g > cap) g = cap;
-    if (g < 1) g = 1;
-    return (int)g;
-}
-
 extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
 {
     long ldk = (k + 3) & ~3;   // 16-byte rows for the vectorised SpMM
@@ -242,16 +234,27 @@ extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
 #define VB_THREADS 256
 #define VB_ROWS 16                                   // row slots of a block, 64 columns per column tile
 
-static int vec_blocks(gcge_gpu_ctx *ctx, int n)
+// Blocks of a grid-stride kernel of the fused rounds: the blocks that are resident
+// at once (its occupancy at VB_THREADS threads, times the SMs) divided over the
+// column tiles, so that every block is in the first wave -- a grid one block per
+// SM past that leaves those blocks running alone after the others finish.
+static int vec_blocks(gcge_gpu_ctx *ctx, const void *fn, int n, int ctiles)
 {
-    long g = cdiv(n > 0 ? n : 1, RED_ROWS), cap = (long)ctx->num_sms * 6;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, VB_THREADS, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    long g = cdiv(n > 0 ? n : 1, RED_ROWS), cap = (long)ctx->num_sms * per_sm / (ctiles > 0 ? ctiles : 1);
+    if (cap < 1) cap = 1;
     return (int)(g < cap ? g : cap);
 }
 
 // sum the per-thread column partials s[4] (thread (rs, cg) holds columns
-// c0 + 4 cg .. +3 of its row slot) over the row slots in a fixed order
+// c0 + 4 cg .. +3 of its row slot) over the row slots in a fixed order; the block's
+// partials of the kact active columns go to row blockIdx.x of part (row stride k,
+// the layout that the column-sum kernels read)
 template <int SLOTS, int COLS>
-__device__ __forceinline__ void vb_block_reduce(const double s[4], int slot, int cg, int c0, int k, double *part)
+__device__ __forceinline__ void vb_block_reduce(const double s[4], int slot, int cg, int c0, int kact, int k,
+                                                double *part)
 {
     __shared__ double red[SLOTS][COLS + 1];
 #pragma unroll
@@ -260,7 +263,7 @@ __device__ __forceinline__ void vb_block_reduce(const double s[4], int slot, int
     for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
         double t = 0;
         for (int r = 0; r < SLOTS; ++r) t += red[r][c];
-        if (c0 + c < k) part[(long)blockIdx.x * k + c0 + c] = t;
+        if (c0 + c < kact) part[(long)blockIdx.x * k + c0 + c] = t;
     }
 }
 
@@ -349,75 +352,108 @@ k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const 
 #pragma unroll
         for (int q = 0; q < 4; ++q) s[q] += (double)run[q];
     }
-    vb_block_reduce<VB_ROWS, 64>(s, rs, cg, blockIdx.y * 64, ka, part);
+    vb_block_reduce<VB_ROWS, 64>(s, rs, cg, blockIdx.y * 64, ka, k, part);
 }
 
 // W = A P (FP32, the first nact columns) and block partials of p.w: L lanes per
-// row, 4 columns per lane, 256 / L rows per block pass; grid-stride over rows
-// (measured faster than contiguous row ranges per block on the Q1 cube)
-template <int L>
-__global__ void __launch_bounds__(VB_THREADS)
+// row, NV float4 column groups per lane (lane l owns columns 4l + 4Lv .. +3, so
+// that each group load of the L lanes reads one contiguous 16L-byte run), 256 / L
+// rows per block pass; grid-stride over rows (measured faster than contiguous row
+// ranges per block on the Q1 cube). NV = 2 halves the shuffles and address
+// arithmetic per FMA. The p.w products are summed in FP32 over runs of 8 rows of
+// a row slot and the runs added in FP64 to the slot's shared-memory partials
+// (the thread's own entries: no atomics, fixed order).
+template <int L, int NV>
+__global__ void __launch_bounds__(VB_THREADS, 5)                  // 48 registers: 5 blocks per SM
 k_spmm32_dot(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
              const float *__restrict__ P, float *__restrict__ W, long ld, int k, const int *__restrict__ nact,
              double *__restrict__ part)
 {
-    constexpr int RPB = VB_THREADS / L;
+    constexpr int RPB = VB_THREADS / L, COLS = 4 * L * NV, UNR = NV == 1 ? 4 : 2;
+    __shared__ double red[RPB][COLS + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / L, sl = lane % L;
     const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (sub * L));
     const int slot = warp * (32 / L) + sub;
     const int kact = min(*nact, k);
-    const int c = 4 * sl;
-    double s[4] = {0, 0, 0, 0};
-    float run[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) red[slot][4 * sl + 4 * L * v + q] = 0.0;
+    float run[4 * NV];
+#pragma unroll
+    for (int q = 0; q < 4 * NV; ++q) run[q] = 0.f;
     int cnt = 0;
     if (kact > 0)
         for (long row = (long)blockIdx.x * RPB + slot; row < n; row += (long)gridDim.x * RPB) {
             const int beg = rp[row], end = rp[row + 1];
-            float acc[4] = {0, 0, 0, 0};
+            float acc[4 * NV];
+#pragma unroll
+            for (int q = 0; q < 4 * NV; ++q) acc[q] = 0.f;
             for (int base = beg; base < end; base += L) {
                 const int e = base + sl;
                 int j = 0;
                 float a = 0.f;
                 if (e < end) { j = __ldg(ci + e); a = __ldg(val + e); }
                 const int m = min(L, end - base);
-#pragma unroll 4
+#pragma unroll UNR
                 for (int t = 0; t < m; ++t) {
                     const int jj = __shfl_sync(gmask, j, t, L);
                     const float aa = __shfl_sync(gmask, a, t, L);
-                    if (c < kact) {
-                        const float4 xv = __ldg(reinterpret_cast<const float4 *>(P + (long)jj * ld + c));
-                        acc[0] = fmaf(aa, xv.x, acc[0]); acc[1] = fmaf(aa, xv.y, acc[1]);
-                        acc[2] = fmaf(aa, xv.z, acc[2]); acc[3] = fmaf(aa, xv.w, acc[3]);
-                    }
+                    const float *xr = P + (long)jj * ld + 4 * sl;
+#pragma unroll
+                    for (int v = 0; v < NV; ++v)
+                        if (4 * sl + 4 * L * v < kact) {
+                            const float4 xv = __ldg(reinterpret_cast<const float4 *>(xr + 4 * L * v));
+                            acc[4 * v + 0] = fmaf(aa, xv.x, acc[4 * v + 0]);
+                            acc[4 * v + 1] = fmaf(aa, xv.y, acc[4 * v + 1]);
+                            acc[4 * v + 2] = fmaf(aa, xv.z, acc[4 * v + 2]);
+                            acc[4 * v + 3] = fmaf(aa, xv.w, acc[4 * v + 3]);
+                        }
                 }
             }
-            if (c < kact) {
-                const long o = row * ld + c;
-                const float4 pv = *reinterpret_cast<const float4 *>(P + o);
-                const float *pe = &pv.x;
-                float4 *wp = reinterpret_cast<float4 *>(W + o);
-                if (c + 4 <= kact) {
-                    *wp = make_float4(acc[0], acc[1], acc[2], acc[3]);
-                } else {
-                    float *we = reinterpret_cast<float *>(wp);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const int c = 4 * sl + 4 * L * v;
+                if (c < kact) {
+                    const long o = row * ld + c;
+                    const float4 pv = *reinterpret_cast<const float4 *>(P + o);
+                    const float *pe = &pv.x;
+                    float4 *wp = reinterpret_cast<float4 *>(W + o);
+                    if (c + 4 <= kact) {
+                        *wp = make_float4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+                    } else {
+                        float *we = reinterpret_cast<float *>(wp);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (c + q < kact) we[q] = acc[4 * v + q];
+                    }
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
-                        if (c + q < kact) we[q] = acc[q];
+                        if (c + q < kact) run[4 * v + q] = fmaf(pe[q], acc[4 * v + q], run[4 * v + q]);
                 }
+            }
+            if (++cnt == 8) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (c + q < kact) run[q] = fmaf(pe[q], acc[q], run[q]);
-                if (++cnt == 8) {
+                for (int v = 0; v < NV; ++v)
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) { s[q] += (double)run[q]; run[q] = 0.f; }
-                    cnt = 0;
-                }
+                    for (int q = 0; q < 4; ++q) {
+                        red[slot][4 * sl + 4 * L * v + q] += (double)run[4 * v + q];
+                        run[4 * v + q] = 0.f;
+                    }
+                cnt = 0;
             }
         }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) s[q] += (double)run[q];
-    vb_block_reduce<RPB, 4 * L>(s, slot, sl, 0, kact, part);
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) red[slot][4 * sl + 4 * L * v + q] += (double)run[4 * v + q];
+    __syncthreads();
+    for (int c = threadIdx.x; c < COLS; c += blockDim.x) {
+        double t = 0;
+        for (int r = 0; r < RPB; ++r) t += red[r][c];
+        if (c < kact) part[(long)blockIdx.x * k + c] = t;
+    }
 }
 
 // column sums of the block partials (one block per active column, fixed order)
@@ -478,28 +514,39 @@ k_colsum_finalize(int nblk, int k, const double *__restrict__ part, double *sums
 static int bcg_rounds32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, float *R, float *X, float *P, float *W, long ld,
                         const gb_bcg_args *a, bcg_state *s)
 {
-    const int n = a->n, k = a->k, G = vec_blocks(ctx, n);
+    const int n = a->n, k = a->k;
     const int ctiles = (k + 63) / 64;
-    const int L = k <= 16 ? 4 : (k <= 32 ? 8 : (k <= 64 ? 16 : 32));
+    // lanes per row and float4 groups per lane: 8 L NV >= k columns (k <= 16: one group)
+    const int L = k <= 16 ? 4 : (k <= 32 ? 4 : (k <= 64 ? 8 : 16));
     if (k > 128 || !A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    const void *spmm_fn = k <= 16 ? (const void *)k_spmm32_dot<4, 1>
+                        : L == 4 ? (const void *)k_spmm32_dot<4, 2>
+                        : L == 8 ? (const void *)k_spmm32_dot<8, 2> : (const void *)k_spmm32_dot<16, 2>;
+    const int Gp = vec_blocks(ctx, (const void *)k_pupdate_v, n, ctiles);
+    const int Gs = vec_blocks(ctx, spmm_fn, n, 1);
+    const int Gx = vec_blocks(ctx, (const void *)k_xr_update_v, n, ctiles);
     for (int it = 1; it < a->max_it; ++it) {
         GB_PROF(ctx, GB_K_BCGVEC, 12.0 * n * k, 2.0 * n * k);
-        GB_LAUNCH(ctx, k_pupdate_v, dim3(G, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
+        GB_LAUNCH(ctx, k_pupdate_v, dim3(Gp, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
         ctx->spmm_launches++;
         GB_PROF(ctx, GB_K_SPMM32, 8.0 * A->nnz + 4.0 * (A->n + 1) + 12.0 * A->n * k, 2.0 * A->nnz * k + 2.0 * A->n * k);
-        if (L == 4)
-            GB_LAUNCH(ctx, k_spmm32_dot<4>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
+        if (k <= 16)
+            GB_LAUNCH(ctx, (k_spmm32_dot<4, 1>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
+                      s->part);
+        else if (L == 4)
+            GB_LAUNCH(ctx, (k_spmm32_dot<4, 2>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
+                      s->part);
         else if (L == 8)
-            GB_LAUNCH(ctx, k_spmm32_dot<8>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
-        else if (L == 16)
-            GB_LAUNCH(ctx, k_spmm32_dot<16>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
+            GB_LAUNCH(ctx, (k_spmm32_dot<8, 2>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
+                      s->part);
         else
-            GB_LAUNCH(ctx, k_spmm32_dot<32>, G, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
-        GB_LAUNCH(ctx, k_colsum_alpha, k, 256, 0, G, k, s->part, s->nact, s->rho2, s->ptw, s->alpha);
+            GB_LAUNCH(ctx, (k_spmm32_dot<16, 2>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
+                      s->part);
+        GB_LAUNCH(ctx, k_colsum_alpha, k, 256, 0, Gs, k, s->part, s->nact, s->rho2, s->ptw, s->alpha);
         GB_PROF(ctx, GB_K_BCGVEC, 24.0 * n * k, 6.0 * n * k);
-        GB_LAUNCH(ctx, k_xr_update_v, dim3(G, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact,
+        GB_LAUNCH(ctx, k_xr_update_v, dim3(Gx, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact,
                   s->part);
-        GB_LAUNCH(ctx, k_colsum_finalize, 1, 1024, 0, G, k, s->part, s->sums, s->rho1, s->rho2, s->err, s->nact,
+        GB_LAUNCH(ctx, k_colsum_finalize, 1, 1024, 0, Gx, k, s->part, s->sums, s->rho1, s->rho2, s->err, s->nact,
                   a->rate, s->beta);
     }
     return GCGE_GPU_OK;

@@ -144,6 +144,27 @@ def test_bcg_fp32_close_to_fp64(ctx):
     assert rel(out[1][0], out[0][0]) < 1e-3
 
 
+@pytest.mark.parametrize("k,max_it,rate", [(4, 10, 1e-2), (10, 10, 1e-2), (10, 5, 1e-1), (20, 8, 1e-2),
+                                            (40, 8, 1e-2), (70, 6, 1e-1)])
+def test_bcg_fp32_tracks_fp64_while_columns_deactivate(ctx, k, max_it, rate):
+    """Columns of very different difficulty leave the active range at different
+    rounds; the FP32 rounds' per-block partials must stay aligned with the column
+    sums over the full column range, so the FP32 iterate keeps FP32 accuracy."""
+    A, _ = P.laplace2d(40, 30)
+    Asp = A.to_scipy()
+    rng = np.random.default_rng(100 + k)
+    R0 = rng.standard_normal((A.n, k)) * np.logspace(0, -3, k)
+    R0[:, ::3] = Asp @ rng.standard_normal((A.n, (k + 2) // 3))
+    dA = ctx.matrix(A, keep_fp32=True)
+    out = []
+    for prec in (0, 1):
+        r, w = ctx.multivec(A.n, k, R0), ctx.multivec(A.n, k)
+        G.bcg(dA, r, 0, w, 0, k, cg_max_it=max_it, cg_rate=rate, precision=prec)
+        out.append(w.download())
+    assert np.all(np.isfinite(out[1]))
+    assert rel(out[1], out[0]) < 1e-4
+
+
 @pytest.mark.parametrize("use_b", [False, True])
 def test_orthonormalize(ctx, use_b):
     Aa, Bb = P.fem_q1_cube(12)
