@@ -232,7 +232,6 @@ extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
 // p update, SpMM with the p.w partials in its epilogue, alpha, x/r update with
 // the r.r partials, beta and the active count.
 #define VB_THREADS 256
-#define VB_ROWS 16                                   // row slots of a block, 64 columns per column tile
 
 // Blocks of a grid-stride kernel of the fused rounds: the blocks that are resident
 // at once (its occupancy at VB_THREADS threads, times the SMs) divided over the
@@ -267,20 +266,27 @@ __device__ __forceinline__ void vb_block_reduce(const double s[4], int slot, int
     }
 }
 
+// The vector kernels of the fused rounds: TPR threads per row (1, 2, 4, 8 or 16,
+// the fewest whose float4 groups cover k, 16 with 64-column tiles over blockIdx.y
+// beyond 64 columns), 4 columns per thread, 256 / TPR rows per block pass; a warp
+// reads 32 TPR-thread row segments, one contiguous run when 4 TPR = ld.
+
 // p = r + beta p (p = r on the first round) on the active columns
+template <int TPR>
 __global__ void __launch_bounds__(VB_THREADS)
 k_pupdate_v(int n, int k, const float *__restrict__ R, float *__restrict__ P, long ld,
             const double *__restrict__ beta, const int *__restrict__ nact, int first)
 {
+    constexpr int RPB = VB_THREADS / TPR;
     const int ka = min(*nact, k);
-    const int cg = threadIdx.x & 15, rs = threadIdx.x >> 4;
+    const int cg = threadIdx.x % TPR, rs = threadIdx.x / TPR;
     const int c0 = blockIdx.y * 64 + 4 * cg;
     if (c0 >= ka) return;
     float b[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) b[q] = (!first && c0 + q < ka) ? (float)beta[c0 + q] : 0.f;
     const bool full = c0 + 4 <= ka;
-    for (long r = (long)blockIdx.x * VB_ROWS + rs; r < n; r += (long)gridDim.x * VB_ROWS) {
+    for (long r = (long)blockIdx.x * RPB + rs; r < n; r += (long)gridDim.x * RPB) {
         const float4 rv = *reinterpret_cast<const float4 *>(R + r * ld + c0);
         float4 *pp = reinterpret_cast<float4 *>(P + r * ld + c0);
         if (first) {                               // p = r: the old p (uninitialised) is not read
@@ -312,13 +318,15 @@ k_pupdate_v(int n, int k, const float *__restrict__ R, float *__restrict__ P, lo
 
 // x += alpha p, r -= alpha w on the active columns, with block partials of r.r
 // (FP32 products summed over runs of 8 rows, the runs summed in FP64)
+template <int TPR>
 __global__ void __launch_bounds__(VB_THREADS)
 k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const float *__restrict__ P,
               const float *__restrict__ W, long ld, const double *__restrict__ alpha, const int *__restrict__ nact,
               double *__restrict__ part)
 {
+    constexpr int RPB = VB_THREADS / TPR;
     const int ka = min(*nact, k);
-    const int cg = threadIdx.x & 15, rs = threadIdx.x >> 4;
+    const int cg = threadIdx.x % TPR, rs = threadIdx.x / TPR;
     const int c0 = blockIdx.y * 64 + 4 * cg;
     double s[4] = {0, 0, 0, 0};
     if (c0 < ka) {
@@ -327,7 +335,7 @@ k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const 
         for (int q = 0; q < 4; ++q) a[q] = c0 + q < ka ? (float)alpha[c0 + q] : 0.f;
         float run[4] = {0, 0, 0, 0};
         int cnt = 0;
-        for (long r = (long)blockIdx.x * VB_ROWS + rs; r < n; r += (long)gridDim.x * VB_ROWS) {
+        for (long r = (long)blockIdx.x * RPB + rs; r < n; r += (long)gridDim.x * RPB) {
             const long o = r * ld + c0;
             float4 xv = *reinterpret_cast<const float4 *>(X + o);
             float4 rv = *reinterpret_cast<const float4 *>(R + o);
@@ -352,7 +360,7 @@ k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const 
 #pragma unroll
         for (int q = 0; q < 4; ++q) s[q] += (double)run[q];
     }
-    vb_block_reduce<VB_ROWS, 64>(s, rs, cg, blockIdx.y * 64, ka, k, part);
+    vb_block_reduce<RPB, 4 * TPR>(s, rs, cg, blockIdx.y * 64, ka, k, part);
 }
 
 // W = A P (FP32, the first nact columns) and block partials of p.w: L lanes per
@@ -511,41 +519,39 @@ k_colsum_finalize(int nblk, int k, const double *__restrict__ part, double *sums
     if (threadIdx.x == 0) *nact = cnt;
 }
 
+typedef void (*pupdate_fn)(int, int, const float *, float *, long, const double *, const int *, int);
+typedef void (*spmm32_fn)(int, const int *, const int *, const float *, const float *, float *, long, int,
+                          const int *, double *);
+typedef void (*xr_fn)(int, int, float *, float *, const float *, const float *, long, const double *, const int *,
+                      double *);
+
 static int bcg_rounds32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, float *R, float *X, float *P, float *W, long ld,
                         const gb_bcg_args *a, bcg_state *s)
 {
     const int n = a->n, k = a->k;
-    const int ctiles = (k + 63) / 64;
-    // lanes per row and float4 groups per lane: 8 L NV >= k columns (k <= 16: one group)
-    const int L = k <= 16 ? 4 : (k <= 32 ? 4 : (k <= 64 ? 8 : 16));
     if (k > 128 || !A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
-    const void *spmm_fn = k <= 16 ? (const void *)k_spmm32_dot<4, 1>
-                        : L == 4 ? (const void *)k_spmm32_dot<4, 2>
-                        : L == 8 ? (const void *)k_spmm32_dot<8, 2> : (const void *)k_spmm32_dot<16, 2>;
-    const int Gp = vec_blocks(ctx, (const void *)k_pupdate_v, n, ctiles);
-    const int Gs = vec_blocks(ctx, spmm_fn, n, 1);
-    const int Gx = vec_blocks(ctx, (const void *)k_xr_update_v, n, ctiles);
+    const int ctiles = (k + 63) / 64;
+    // vector kernels: threads per row whose float4 groups cover k; SpMM: L lanes per
+    // row with NV float4 groups each, 4 L NV >= k
+    const int tpr = k <= 4 ? 1 : (k <= 8 ? 2 : (k <= 16 ? 4 : (k <= 32 ? 8 : 16)));
+    const pupdate_fn pup = tpr == 1 ? k_pupdate_v<1> : tpr == 2 ? k_pupdate_v<2> : tpr == 4 ? k_pupdate_v<4>
+                         : tpr == 8 ? k_pupdate_v<8> : k_pupdate_v<16>;
+    const xr_fn xru = tpr == 1 ? k_xr_update_v<1> : tpr == 2 ? k_xr_update_v<2> : tpr == 4 ? k_xr_update_v<4>
+                    : tpr == 8 ? k_xr_update_v<8> : k_xr_update_v<16>;
+    const spmm32_fn spm = k <= 4 ? k_spmm32_dot<1, 1> : k <= 8 ? k_spmm32_dot<2, 1> : k <= 16 ? k_spmm32_dot<4, 1>
+                        : k <= 32 ? k_spmm32_dot<4, 2> : k <= 64 ? k_spmm32_dot<8, 2> : k_spmm32_dot<16, 2>;
+    const int Gp = vec_blocks(ctx, (const void *)pup, n, ctiles);
+    const int Gs = vec_blocks(ctx, (const void *)spm, n, 1);
+    const int Gx = vec_blocks(ctx, (const void *)xru, n, ctiles);
     for (int it = 1; it < a->max_it; ++it) {
         GB_PROF(ctx, GB_K_BCGVEC, 12.0 * n * k, 2.0 * n * k);
-        GB_LAUNCH(ctx, k_pupdate_v, dim3(Gp, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
+        GB_LAUNCH(ctx, pup, dim3(Gp, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
         ctx->spmm_launches++;
         GB_PROF(ctx, GB_K_SPMM32, 8.0 * A->nnz + 4.0 * (A->n + 1) + 12.0 * A->n * k, 2.0 * A->nnz * k + 2.0 * A->n * k);
-        if (k <= 16)
-            GB_LAUNCH(ctx, (k_spmm32_dot<4, 1>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
-                      s->part);
-        else if (L == 4)
-            GB_LAUNCH(ctx, (k_spmm32_dot<4, 2>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
-                      s->part);
-        else if (L == 8)
-            GB_LAUNCH(ctx, (k_spmm32_dot<8, 2>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
-                      s->part);
-        else
-            GB_LAUNCH(ctx, (k_spmm32_dot<16, 2>), Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact,
-                      s->part);
+        GB_LAUNCH(ctx, spm, Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
         GB_LAUNCH(ctx, k_colsum_alpha, k, 256, 0, Gs, k, s->part, s->nact, s->rho2, s->ptw, s->alpha);
         GB_PROF(ctx, GB_K_BCGVEC, 24.0 * n * k, 6.0 * n * k);
-        GB_LAUNCH(ctx, k_xr_update_v, dim3(Gx, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact,
-                  s->part);
+        GB_LAUNCH(ctx, xru, dim3(Gx, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part);
         GB_LAUNCH(ctx, k_colsum_finalize, 1, 1024, 0, Gx, k, s->part, s->sums, s->rho1, s->rho2, s->err, s->nact,
                   a->rate, s->beta);
     }

@@ -210,25 +210,37 @@ __device__ __forceinline__ void tc_release(tc_hdr *h, uint32_t tmem, int mma_war
 // ---------------------------------------------------------------- Gram column scales
 // exps[c] = smallest e with |X[r, c]| < 2^e for all rows (OZ_NO_EXP for an
 // all-zero column; subnormal entries count as zero). exps must hold OZ_NO_EXP
-// on entry; each block reduces its rows first and issues one atomic per column.
+// on entry. A warp reads whole rows (lane l: columns c0 + l + 32 j, 8 independent
+// loads per row in flight) over 256-column chunks, so each row's bytes stream
+// once per chunk; each block reduces its warps and issues one atomic per column.
+#define CE_COLS 256
 __global__ void __launch_bounds__(256)
 k_col_exponent(int n, int k, const double *__restrict__ X, long ldx, int *__restrict__ exps)
 {
-    __shared__ int se[8][32];
+    __shared__ int se[8][CE_COLS];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long nw = ((long)gridDim.x * blockDim.x) >> 5;
-    for (int c0 = 0; c0 < k; c0 += 32) {
-        const int c = c0 + lane;
-        int e = OZ_NO_EXP;
-        if (c < k)
-            for (long r = warp; r < n; r += nw) e = max(e, oz_exponent(X[r * ldx + c]));
-        se[w][lane] = e;
-        __syncthreads();
-        if (w == 0) {
+    for (int c0 = 0; c0 < k; c0 += CE_COLS) {
+        int e[CE_COLS / 32];
 #pragma unroll
-            for (int q = 1; q < 8; ++q) e = max(e, se[q][lane]);
-            if (c < k && e > OZ_NO_EXP) atomicMax(exps + c, e);
+        for (int j = 0; j < CE_COLS / 32; ++j) e[j] = OZ_NO_EXP;
+        for (long r = warp; r < n; r += nw) {
+            const double *xr = X + r * ldx + c0 + lane;
+            double v[CE_COLS / 32];
+#pragma unroll
+            for (int j = 0; j < CE_COLS / 32; ++j) v[j] = c0 + lane + 32 * j < k ? __ldg(xr + 32 * j) : 0.0;
+#pragma unroll
+            for (int j = 0; j < CE_COLS / 32; ++j) e[j] = max(e[j], oz_exponent(v[j]));
+        }
+#pragma unroll
+        for (int j = 0; j < CE_COLS / 32; ++j) se[w][lane + 32 * j] = e[j];
+        __syncthreads();
+        for (int c = threadIdx.x; c < CE_COLS; c += blockDim.x) {
+            int m = se[0][c];
+#pragma unroll
+            for (int q = 1; q < 8; ++q) m = max(m, se[q][c]);
+            if (c0 + c < k && m > OZ_NO_EXP) atomicMax(exps + c0 + c, m);
         }
         __syncthreads();
     }
@@ -267,6 +279,12 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
     const int nst = (int)((re - rb + TC_KS - 1) / TC_KS);
     const int N = min(TC_N, (k2 - j0 + 15) & ~15);
     tc_setup(h);
+    // digit planes of both buffers start at zero: core matrices wholly outside the
+    // columns of V or W (the padding of a short tile) are never split and keep
+    // zero digits; the split threads' first proxy fence covers these writes
+    if (tid < TC_SPLIT_THREADS)
+        for (int i = tid; i < 2 * TC_STAGE / 16; i += TC_SPLIT_THREADS)
+            reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0u, 0u, 0u, 0u);
     tc_fence_before_sync();
     __syncthreads();
     tc_fence_after_sync();
@@ -315,9 +333,9 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
 #pragma unroll
             for (int cc = 0; cc < GR_CORES_PER_WARP; ++cc) {
                 const int q = warp + TC_SPLIT_WARPS * cc;
-                if (q < TC_ACORES + TC_BCORES) {
-                    const bool isA = q < TC_ACORES;
-                    const int qq = isA ? q : q - TC_ACORES;
+                const bool isA = q < TC_ACORES;
+                const int qq = isA ? q : q - TC_ACORES;
+                if (q < TC_ACORES + TC_BCORES && (isA ? i0 : j0) + 8 * (qq >> 2) < (isA ? k1 : k2)) {
                     const int col = (isA ? i0 : j0) + 8 * (qq >> 2) + i8;
                     const int e = col < (isA ? k1 : k2) ? (isA ? ev : ew)[col] : OZ_NO_EXP;
                     const unsigned long long u0 = oz_bias(xv[cc][0], e), u1 = oz_bias(xv[cc][1], e);

@@ -144,8 +144,8 @@ def test_bcg_fp32_close_to_fp64(ctx):
     assert rel(out[1][0], out[0][0]) < 1e-3
 
 
-@pytest.mark.parametrize("k,max_it,rate", [(4, 10, 1e-2), (10, 10, 1e-2), (10, 5, 1e-1), (20, 8, 1e-2),
-                                            (40, 8, 1e-2), (70, 6, 1e-1)])
+@pytest.mark.parametrize("k,max_it,rate", [(2, 8, 1e-2), (4, 10, 1e-2), (7, 10, 1e-2), (10, 10, 1e-2),
+                                            (10, 5, 1e-1), (20, 8, 1e-2), (40, 8, 1e-2), (70, 6, 1e-1)])
 def test_bcg_fp32_tracks_fp64_while_columns_deactivate(ctx, k, max_it, rate):
     """Columns of very different difficulty leave the active range at different
     rounds; the FP32 rounds' per-block partials must stay aligned with the column
