@@ -514,9 +514,13 @@ k_lc_coef_split(int k1, int k2, const double *__restrict__ C, int ldc, int upper
 // with one TMEM allocation and one barrier set; the stage counter runs across
 // tiles. While the K stages of a tile run, the split warps also load the next
 // tile's entries of the same stage and fold their exponents into that tile's row
-// scales (shared-memory atomicMax), so only the first tile has a separate scale
-// pass and every later tile's X is already in L2 when it is split. The drain
-// writes Y directly.
+// scales (shared-memory atomicMax) one stage later, when the loads have landed,
+// so only the first tile has a separate scale pass and every later tile's X is
+// already in L2 when it is split. The drain
+// writes Y directly. MULTI: the inner dimension is longer than one exact
+// accumulation (k1 > OZ_EXACT_TERMS) and the drained chunks are summed in
+// registers; the single-chunk form holds no FP64 accumulators while it splits.
+template <bool MULTI>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, const uint4 *__restrict__ Bd,
              const int *__restrict__ g_in, const int *__restrict__ ec, double alpha, double beta,
@@ -598,6 +602,29 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
         }
     };
     if (!mma_warp) load_stage((long)blockIdx.x * TC_M, 0);
+    // high words (sign, exponent) of the next tile's entries of one stage, in flight
+    unsigned pw[LC_CORES_PER_WARP][2];
+    int pw_stage = -1;
+    auto fold_scales = [&](int ps) {
+        const int ib = ps * TC_KS + 2 * kp;
+#pragma unroll
+        for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
+            const int q = warp + TC_SPLIT_WARPS * cc;
+            if (q < TC_ACORES) {
+                const int i = ib + 8 * (q & 3);
+                int e = OZ_NO_EXP;
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int ex = (int)((pw[cc][u] >> 20) & 0x7ff);
+                    const int gi = i + u < k1 ? gs[i + u] : OZ_NO_EXP;
+                    if (ex && gi != OZ_NO_EXP) e = max(e, ex - 1022 + gi);
+                }
+                e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
+                e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
+                if (kp == 0 && e > OZ_NO_EXP) atomicMax(er_next + 8 * (q >> 2) + r8, e);
+            }
+        }
+    };
 
     int gsc = 0;                                         // stages issued by this CTA, over all tiles
     bool stop = false;
@@ -605,9 +632,9 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
         const long row0 = t * TC_M, nrow0 = row0 + (long)gridDim.x * TC_M;
         const bool has_next = t + gridDim.x < ntiles;
         const int my_e = er[my_row];
-        double acc[TC_COLS_PER_WARP];
+        double acc[MULTI ? TC_COLS_PER_WARP : 1];
 #pragma unroll
-        for (int q = 0; q < TC_COLS_PER_WARP; ++q) acc[q] = 0.0;
+        for (int q = 0; q < (MULTI ? TC_COLS_PER_WARP : 1); ++q) acc[q] = 0.0;
         for (int s = 0; s < nst; ++s, ++gsc) {
             const int buf = gsc & 1, cs = s % chunk_stages;
             const bool chunk_end = cs == chunk_stages - 1 || s == nst - 1;
@@ -651,8 +678,12 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
                 // tile's first stage), and the next tile's entries of this stage for its scales
                 if (s + 1 < nst) load_stage(row0, s + 1);
                 else if (has_next) load_stage(nrow0, 0);
+                // the next tile's high words of the previous stage arrived while this
+                // stage was split: fold them into its row scales now, then issue this
+                // stage's (consumed one stage later, so no load latency is waited on)
+                if (pw_stage >= 0) fold_scales(pw_stage);
+                pw_stage = -1;
                 if (has_next) {
-                    unsigned w[LC_CORES_PER_WARP][2];
 #pragma unroll
                     for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
                         const int q = warp + TC_SPLIT_WARPS * cc;
@@ -660,26 +691,10 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
                         const int i = ib + 8 * (q & 3);
                         const bool in = q < TC_ACORES && r < n;
                         const unsigned *xh = reinterpret_cast<const unsigned *>(X + (in ? r : 0) * ldx + i) + 1;
-                        w[cc][0] = (in && i < k1) ? __ldg(xh) : 0u;
-                        w[cc][1] = (in && i + 1 < k1) ? __ldg(xh + 2) : 0u;
+                        pw[cc][0] = (in && i < k1) ? __ldg(xh) : 0u;
+                        pw[cc][1] = (in && i + 1 < k1) ? __ldg(xh + 2) : 0u;
                     }
-#pragma unroll
-                    for (int cc = 0; cc < LC_CORES_PER_WARP; ++cc) {
-                        const int q = warp + TC_SPLIT_WARPS * cc;
-                        if (q < TC_ACORES) {
-                            const int i = ib + 8 * (q & 3);
-                            int e = OZ_NO_EXP;
-#pragma unroll
-                            for (int u = 0; u < 2; ++u) {
-                                const int ex = (int)((w[cc][u] >> 20) & 0x7ff);
-                                const int gi = i + u < k1 ? gs[i + u] : OZ_NO_EXP;
-                                if (ex && gi != OZ_NO_EXP) e = max(e, ex - 1022 + gi);
-                            }
-                            e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
-                            e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
-                            if (kp == 0 && e > OZ_NO_EXP) atomicMax(er_next + 8 * (q >> 2) + r8, e);
-                        }
-                    }
+                    pw_stage = s;
                 }
             }
             if (chunk_end) {
@@ -703,11 +718,14 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
                             oz_levels_to_int<LC_LEVELS>(lev, a, b);
                             const double d =
                                 oz_to_double<40>(a, b, my_e + ecs[col0 + g4 * 4 + q] - OZ_SCALE_OFFSET);
-                            acc[g4 * 4 + q] = first ? d : acc[g4 * 4 + q] + d;
+                            double v2 = d;
+                            if (MULTI) {
+                                acc[g4 * 4 + q] = first ? d : acc[g4 * 4 + q] + d;
+                                v2 = acc[g4 * 4 + q];
+                            }
                             const int j = j0 + col0 + g4 * 4 + q;
                             if (last && r < n && j < k2) {
                                 double *y = Y + r * ldy + j;
-                                const double v2 = acc[g4 * 4 + q];
                                 *y = plain ? (alpha == 1.0 ? v2 : -v2) : fma(beta, *y, alpha * v2);
                             }
                         }
@@ -722,7 +740,13 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
                 break;
             }
         }
-        // tile end: every scale atomic of the next tile is done; er <- er_next
+        // tile end: fold the last stage's words (they arrived during the drain); then
+        // every scale atomic of the next tile is done; er <- er_next
+        if (!mma_warp && pw_stage >= 0) {
+            __syncwarp();
+            fold_scales(pw_stage);
+            pw_stage = -1;
+        }
         __syncthreads();
         if (tid < TC_M) {
             er[tid] = er_next[tid];
@@ -743,7 +767,10 @@ extern "C" int gb_lincomb_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const dou
 {
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(k_lincomb_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, LC_SMEM) != cudaSuccess)
+        if (cudaFuncSetAttribute(k_lincomb_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC_SMEM) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_lincomb_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, LC_SMEM) !=
+                cudaSuccess)
             return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
         attr = true;
     }
@@ -761,7 +788,11 @@ extern "C" int gb_lincomb_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const dou
     long P = ctx->num_sms / jtiles;
     if (P < 1) P = 1;
     if (P > ntiles) P = ntiles;
-    GB_LAUNCH(ctx, k_lincomb_tc, dim3((unsigned)P, jtiles), TC_THREADS, LC_SMEM, n, k1, k2, X, ldx, (const uint4 *)Bd,
-              g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err);
+    if (k1 > OZ_EXACT_TERMS)
+        GB_LAUNCH(ctx, k_lincomb_tc<true>, dim3((unsigned)P, jtiles), TC_THREADS, LC_SMEM, n, k1, k2, X, ldx,
+                  (const uint4 *)Bd, g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err);
+    else
+        GB_LAUNCH(ctx, k_lincomb_tc<false>, dim3((unsigned)P, jtiles), TC_THREADS, LC_SMEM, n, k1, k2, X, ldx,
+                  (const uint4 *)Bd, g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err);
     return GCGE_GPU_OK;
 }
