@@ -98,6 +98,8 @@ def load():
         "GCGE_GPU_ProfileRead": (_I, [_P, _I, _P, _P, _P, _P, _I]),
         "GCGE_GPU_SetTensorEmulation": (_I, [_P, _I]),
         "GCGE_GPU_InnerProdNoAlloc": (_I, [_I, _I, _I, _P, C.c_long, _P, C.c_long, _P, _I, _I, _P]),
+        "GCGE_GPU_PatternGrad": (_I, [_P, _P, _I, _P, _I, _I, _P, _I, _P]),
+        "GCGE_GPU_EigvecAdjoint": (_I, [_P, _P, _P, _I, _P, _I, _P, _I, _P, _I, _D, _D, _I, C.POINTER(_I)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -340,6 +342,26 @@ def multivec_swap(V1, V2, start, end):
 
 def bcg(A, RHS, r_start, W, w_start, k, cg_max_it=20, cg_rate=1e-2, precision=0):
     _chk(A.lib.GCGE_GPU_BCG(A.h, RHS.h, r_start, W.h, w_start, k, cg_max_it, cg_rate, precision), "BCG")
+
+
+# ---- differentiation (adjoint kernels)
+def pattern_grad(M, U, u0, V, v0, r, scale, nnz, grad=None):
+    """grad[e] (+)= sum_t scale[t] U[i, u0+t] V[j, v0+t] over the stored entries
+    e = (i, j) of M (CSR order); with grad given, the sums are added to it."""
+    sc = _arr(scale, np.float64)
+    acc = grad is not None
+    g = np.zeros(nnz) if grad is None else grad
+    _chk(M.lib.GCGE_GPU_PatternGrad(M.h, U.h, u0, V.h, v0, r, _ptr(sc), int(acc), _ptr(g)), "PatternGrad")
+    return g
+
+
+def eigvec_adjoint(A, B, X, m, eval_, k, G, g_col, MU, mu_col, cluster_tol=1e-10, tol=1e-12, max_it=2000):
+    """mu (column mu_col of MU) of the eigenvector functional adjoint; returns the CG iterations."""
+    ev = _arr(eval_, np.float64)
+    it = C.c_int(0)
+    _chk(A.lib.GCGE_GPU_EigvecAdjoint(A.h, B.h if B is not None else None, X.h, m, _ptr(ev), k, G.h, g_col, MU.h,
+                                      mu_col, cluster_tol, tol, max_it, C.byref(it)), "EigvecAdjoint")
+    return it.value
 
 
 def orthonormalize(W, start, end, B=None, max_reorth_time=3, orth_zero_tol=1e-16):

@@ -200,6 +200,38 @@ int  GCGE_GPU_ProfileEnable(gcge_gpu_ctx *ctx, int on);
 int  GCGE_GPU_ProfileRead(gcge_gpu_ctx *ctx, int nclass, double *ms, long long *launches,
                           double *bytes, double *flops, int reset);
 
+/* ---- 5. differentiation (adjoint kernels; no counterpart in the reference) ----
+ *
+ * Gradients of a function of computed eigenpairs with respect to the stored
+ * entries of A and B. Each stored entry (i, j) is one independent variable (a
+ * symmetric perturbation of an off-diagonal pair is the sum of the gradients of
+ * the two stored entries). For a B-orthonormal eigenpair (lambda, x):
+ *   d lambda / d A_ij = x_i x_j,  d lambda / d B_ij = -lambda x_i x_j;
+ * for a function L of a simple eigenvector x with g = dL/dx and mu from
+ * GCGE_GPU_EigvecAdjoint:
+ *   dL / d A_ij = -mu_i x_j,  dL / d B_ij = lambda mu_i x_j - (g^T x / 2) x_i x_j. */
+
+/* grad[e] = sum_t scale[t] U(i, u0+t) V(j, v0+t) over t < r for every stored
+ * entry e = (i, j) of M, in M's CSR order (accumulate != 0: added to grad).
+ * grad: host array of nnz(M) doubles; scale: host array of r doubles;
+ * r <= 768. */
+int  GCGE_GPU_PatternGrad(const gcge_gpu_mat *M, const gcge_gpu_mv *U, int u0, const gcge_gpu_mv *V,
+                          int v0, int r, const double *scale, int accumulate, double *grad);
+
+/* mu (column mu_col of MU) solving (A - lambda_k B) mu = (I - B x_k x_k^T) g with
+ * x_k^T B mu = 0, for the eigenpair (lambda_k, x_k) = (eval[k], X(:, k)) of the
+ * B-orthonormal eigenvectors X(:, 0:m) (eval: host array of m values; B may be
+ * NULL: B = I) and g = column g_col of G. The components along the other x_j are
+ * x_j (x_j^T g) / (lambda_j - lambda_k), except inside k's cluster
+ * (|lambda_j - lambda_k| <= cluster_tol |lambda_k|, left at zero); the rest
+ * solves the shifted system on the B-complement of X(:, 0:m), where it is
+ * positive definite when lambda_k is below the first eigenvalue not in X, by
+ * FP64 conjugate gradients to relative residual tol in at most max_it
+ * iterations (iters, if not NULL, returns the count). */
+int  GCGE_GPU_EigvecAdjoint(const gcge_gpu_mat *A, const gcge_gpu_mat *B, const gcge_gpu_mv *X, int m,
+                            const double *eval, int k, const gcge_gpu_mv *G, int g_col, gcge_gpu_mv *MU,
+                            int mu_col, double cluster_tol, double tol, int max_it, int *iters);
+
 /* ---- allocation-free Gram product (no counterpart in the reference) ----
  *
  * For callers that own all device memory through their own pool or arena and
