@@ -380,6 +380,8 @@ def run_kernel(args):
     from gcge_gb300 import problems as P
     ctx = G.Context(0)
     rng = np.random.default_rng(0)
+    if args.kernel == "adjoint":
+        return run_adjoint(args, ctx)
     if args.kernel.startswith("spmm"):
         A, B = P.fem_q1_cube(args.ne)
         Msp = A if args.kernel == "spmm_a" else B
@@ -417,6 +419,43 @@ def run_kernel(args):
                       "fp64_equiv_tflops": flops / dt / 1e12 if dt > 0 else None}))
 
 
+def run_adjoint(args, ctx):
+    """The gradient of L = sum of the 20 smallest eigenvalues + sum_r w_r x_1[r]^2
+    for the variable-coefficient 5-point problem on --nc^2 cells (B = I, nev 24):
+    forward mixed-precision solve to residual 1e-8, then the backward pass
+    (pattern gradients over A's stored entries and the eigenvector adjoint solve
+    to relative residual 1e-8), timed separately over --steps repetitions."""
+    import numpy as np
+    import gcge_gb300 as G
+    from gcge_gb300 import problems as P
+    A, _ = P.varcoef2d(nc=args.nc, seed=20240302, sigma=0.5)
+    q, nev, nnz = 20, 24, len(A.val)
+    wvec = np.random.default_rng(20240303).uniform(0.0, 1.0, A.n)
+    dA = ctx.matrix(A, keep_fp32=True)
+    X = ctx.multivec(A.n, nev)
+    params = ctx.params(nev=nev, ev_tol=1e-8, conv_type="BR", ev_max_it=2000, seed=77, precision=1)
+    ctx.sync()
+    t = time.perf_counter()
+    ev, Xh, st = ctx.solve(dA, None, params, evec=X)
+    t_solve = time.perf_counter() - t
+    Gd, MU = ctx.multivec(A.n, 1, 2.0 * wvec * Xh[:, 0]), ctx.multivec(A.n, 1)
+    ones = np.ones(q)
+    times, its = [], []
+    for _ in range(max(args.steps, 1)):
+        ctx.sync()
+        t = time.perf_counter()
+        gA = G.pattern_grad(dA, X, 0, X, 0, q, ones, nnz)
+        its.append(G.eigvec_adjoint(dA, None, X, nev, ev, 0, Gd, 0, MU, 0, tol=1e-8, max_it=20000))
+        G.pattern_grad(dA, MU, 0, X, 0, 1, [-1.0], nnz, grad=gA)
+        ctx.sync()
+        times.append(time.perf_counter() - t)
+    ctx.close()
+    print(json.dumps({"kernel": "adjoint", "shape": "varcoef2d %d^2: n=%d nnz=%d, q=%d, nev=%d" % (
+        args.nc, A.n, nnz, q, nev), "forward_solve_s": t_solve, "forward_iterations": st.num_iter,
+        "backward_s": min(times), "adjoint_cg_iterations": its[-1],
+        "grad_norm": float(np.linalg.norm(gA))}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,11 +468,12 @@ def main():
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "bcg32", "lincomb", "gram"],
+    ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "bcg32", "lincomb", "gram", "adjoint"],
                     help="time one hot operation instead of the solve (profiling)")
     ap.add_argument("--n", type=int, default=262144, help="rows for --kernel lincomb/gram")
     ap.add_argument("--ne", type=int, default=64, help="cube edge for --kernel spmm_a/spmm_b")
     ap.add_argument("--k", type=int, default=64, help="columns for --kernel spmm_a/spmm_b/bcg32")
+    ap.add_argument("--nc", type=int, default=512, help="cells per edge for --kernel adjoint")
     args = ap.parse_args()
     if args.kernel:
         run_kernel(args)

@@ -141,6 +141,107 @@ done:
     return st;
 }
 
+// ---------------------------------------------------------------- single-vector kernels
+// The adjoint CG works on one n-vector at a time; these kernels are sized for
+// that (the block kernels of the solver are not).
+#define AV_THREADS 256
+#define AV_BLOCKS_PER_SM 4
+
+static int av_grid(gcge_gpu_ctx *ctx, long work)
+{
+    long g = (work + AV_THREADS - 1) / AV_THREADS, cap = (long)ctx->num_sms * AV_BLOCKS_PER_SM;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// y = a x + b y (b == 0: y = a x, y not read)
+__global__ void k_av_axpby(long n, double a, const double *__restrict__ x, double b, double *__restrict__ y)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        y[i] = b == 0.0 ? a * x[i] : fma(a, x[i], b * y[i]);
+}
+
+// part[block] = sum over the block's grid-stride slice of x_i y_i (fixed order)
+__global__ void __launch_bounds__(AV_THREADS)
+k_av_dot_part(long n, const double *__restrict__ x, const double *__restrict__ y, double *__restrict__ part)
+{
+    __shared__ double red[AV_THREADS / 32];
+    double s = 0.0;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        s = fma(x[i], y[i], s);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < AV_THREADS / 32; ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// out[0] = sum of nparts partials (one warp, fixed order)
+__global__ void k_av_sum(int nparts, const double *__restrict__ part, double *__restrict__ out)
+{
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += 32) s += part[i];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[0] = s;
+}
+
+// part[block][j] = sum over the block's rows of X[r, j] v[r], j < m <= 64: a warp
+// per row, lanes over the columns (a row of X is contiguous)
+__global__ void __launch_bounds__(AV_THREADS)
+k_av_xtv_part(long n, int m, const double *__restrict__ X, long ldx, const double *__restrict__ v,
+              double *__restrict__ part)
+{
+    __shared__ double red[AV_THREADS / 32][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double s0 = 0.0, s1 = 0.0;
+    const long nw = ((long)gridDim.x * AV_THREADS) >> 5;
+    for (long r = ((long)blockIdx.x * AV_THREADS + threadIdx.x) >> 5; r < n; r += nw) {
+        const double vr = v[r];
+        const double *xr = X + r * ldx;
+        if (lane < m) s0 = fma(xr[lane], vr, s0);
+        if (lane + 32 < m) s1 = fma(xr[lane + 32], vr, s1);
+    }
+    red[w][lane] = s0;
+    red[w][lane + 32] = s1;
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += AV_THREADS) {
+        double t = 0.0;
+        for (int q = 0; q < AV_THREADS / 32; ++q) t += red[q][j];
+        part[(long)blockIdx.x * m + j] = t;
+    }
+}
+
+// c[j] = sum of the partials of column j (thread per column, fixed order)
+__global__ void k_av_xtv_sum(int nparts, int m, const double *__restrict__ part, double *__restrict__ c)
+{
+    const int j = threadIdx.x;
+    if (j >= m) return;
+    double t = 0.0;
+    for (int b = 0; b < nparts; ++b) t += part[(long)b * m + j];
+    c[j] = t;
+}
+
+// y = v - X c (thread per row, c in shared memory), m <= 64
+__global__ void __launch_bounds__(AV_THREADS)
+k_av_v_minus_xc(long n, int m, const double *__restrict__ X, long ldx, const double *__restrict__ c,
+                const double *__restrict__ v, double *__restrict__ y)
+{
+    __shared__ double cs[64];
+    if (threadIdx.x < m) cs[threadIdx.x] = c[threadIdx.x];
+    __syncthreads();
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+        const double *xr = X + r * ldx;
+        double s = 0.0;
+        for (int j = 0; j < m; ++j) s = fma(xr[j], cs[j], s);
+        y[r] = v[r] - s;
+    }
+}
+
 // ---------------------------------------------------------------- adjoint solve
 // Work of one adjoint solve, all device resident (n-vectors contiguous, ld 1).
 struct ad_work {
@@ -148,16 +249,48 @@ struct ad_work {
     double *y, *r, *p, *q, *t, *u, *w;
     double *c;         // m coefficients
     double *dot;       // one scalar
+    double *part;      // block partials (grid x max(m, 1))
     double *h_c;       // host copy of m coefficients
 };
 
+#define AD_SKINNY_M 64                  // widest X handled by the single-vector kernels
+
+static int ad_axpby(gcge_gpu_ctx *ctx, int n, double a, const double *x, double b, double *y)
+{
+    GB_LAUNCH(ctx, k_av_axpby, av_grid(ctx, n), AV_THREADS, 0, (long)n, a, x, b, y);
+    return GCGE_GPU_OK;
+}
+
 static int ad_dot(gcge_gpu_ctx *ctx, int n, const double *x, const double *y, ad_work *W, double *out)
 {
-    int st = gb_col_dots(ctx, n, 1, x, 1, y, 1, W->dot);
-    if (st) return st;
+    const int g = av_grid(ctx, n);
+    GB_LAUNCH(ctx, k_av_dot_part, g, AV_THREADS, 0, (long)n, x, y, W->part);
+    GB_LAUNCH(ctx, k_av_sum, 1, 32, 0, g, W->part, W->dot);
     AD_CUDA(ctx, cudaMemcpyAsync(out, W->dot, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     AD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (!isfinite(*out)) return gb_fail(ctx, GCGE_GPU_ERR_NONFINITE);
+    return GCGE_GPU_OK;
+}
+
+// c = X^T v (m coefficients, device)
+static int ad_xtv(gcge_gpu_ctx *ctx, int n, int m, const double *X, long ldx, const double *v, double *c, ad_work *W)
+{
+    if (m > AD_SKINNY_M) return gb_gram(ctx, n, m, 1, X, ldx, v, 1, c, m, 0);
+    const int g = av_grid(ctx, (long)n * 32);
+    GB_LAUNCH(ctx, k_av_xtv_part, g, AV_THREADS, 0, (long)n, m, X, ldx, v, W->part);
+    GB_LAUNCH(ctx, k_av_xtv_sum, 1, 64, 0, g, m, W->part, c);
+    return GCGE_GPU_OK;
+}
+
+// y = v - X c (y may be v)
+static int ad_v_minus_xc(gcge_gpu_ctx *ctx, int n, int m, const double *X, long ldx, const double *c,
+                         const double *v, double *y)
+{
+    if (m > AD_SKINNY_M) {
+        int st = y != v ? ad_axpby(ctx, n, 1.0, v, 0.0, y) : GCGE_GPU_OK;
+        return st ? st : gb_lincomb(ctx, n, m, 1, X, ldx, c, m, -1.0, 1.0, y, 1, 0);
+    }
+    GB_LAUNCH(ctx, k_av_v_minus_xc, av_grid(ctx, n), AV_THREADS, 0, (long)n, m, X, ldx, c, v, y);
     return GCGE_GPU_OK;
 }
 
@@ -166,10 +299,8 @@ static int ad_dot(gcge_gpu_ctx *ctx, int n, const double *x, const double *y, ad
 static int ad_project(gcge_gpu_ctx *ctx, int n, int m, const double *X, long ldx, const double *Xo, long ldo,
                       const double *src, const double *Bsrc, double *dst, ad_work *W)
 {
-    int st = gb_gram(ctx, n, m, 1, X, ldx, Bsrc, 1, W->c, m, 0);
-    if (!st && dst != src) st = gb_axpby(ctx, n, 1, 1.0, src, 1, 0.0, dst, 1);
-    if (!st) st = gb_lincomb(ctx, n, m, 1, Xo, ldo, W->c, m, -1.0, 1.0, dst, 1, 0);
-    return st;
+    int st = ad_xtv(ctx, n, m, X, ldx, Bsrc, W->c, W);
+    return st ? st : ad_v_minus_xc(ctx, n, m, Xo, ldo, W->c, src, dst);
 }
 
 // q = P^T (A - lambda B) P p with P = I - X X^T B (t, u, w scratch)
@@ -190,8 +321,8 @@ static int ad_apply(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat
     if ((st = gb_spmm(ctx, A, W->t, 1, W->u, 1, 1, 1.0, nullptr, 0.0, nullptr))) return st;
     if (B) {
         if ((st = gb_spmm(ctx, B, W->t, 1, W->w, 1, 1, 1.0, nullptr, 0.0, nullptr))) return st;
-        if ((st = gb_axpby(ctx, n, 1, -lambda, W->w, 1, 1.0, W->u, 1))) return st;
-    } else if ((st = gb_axpby(ctx, n, 1, -lambda, W->t, 1, 1.0, W->u, 1))) {
+        if ((st = ad_axpby(ctx, n, -lambda, W->w, 1.0, W->u))) return st;
+    } else if ((st = ad_axpby(ctx, n, -lambda, W->t, 1.0, W->u))) {
         return st;
     }
     // q = P^T u = u - B X (X^T u)
@@ -213,7 +344,7 @@ static int ad_solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat
     }
     // c = X^T g; explicit components a_j = c_j / (lambda_j - lambda) outside k's cluster
     if ((st = gb_axpby(ctx, n, 1, 1.0, g, ldg, 0.0, W->r, 1))) return st;   // r = g (contiguous)
-    if ((st = gb_gram(ctx, n, m, 1, X, ldx, W->r, 1, W->c, m, 0))) return st;
+    if ((st = ad_xtv(ctx, n, m, X, ldx, W->r, W->c, W))) return st;
     AD_CUDA(ctx, cudaMemcpyAsync(W->h_c, W->c, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream));
     AD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     const double cscale = fmax(fabs(lambda), DBL_MIN);
@@ -221,61 +352,45 @@ static int ad_solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat
     if (!h_a) return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
     for (int j = 0; j < m; ++j) {
         const double gap = eval[j] - lambda;
-        h_a[j] = fabs(gap) <= cluster_tol * cscale ? 0.0 : W->h_c[j] / gap;
+        h_a[j] = fabs(gap) <= cluster_tol * cscale ? 0.0 : -W->h_c[j] / gap;   // negated: v - X c form
     }
-    // b = P^T g = g - B X c  (into r), the right-hand side of the projected system
-    if ((st = gb_lincomb(ctx, n, m, 1, BX, ldbx, W->c, m, -1.0, 1.0, W->r, 1, 0))) {
-        free(h_a);
-        return st;
-    }
-    // CG on P^T (A - lambda B) P y = b from y = 0
-    if ((st = gb_set_zero(ctx, W->y, (size_t)n))) {
-        free(h_a);
-        return st;
-    }
-    if ((st = gb_axpby(ctx, n, 1, 1.0, W->r, 1, 0.0, W->p, 1))) {
-        free(h_a);
-        return st;
-    }
-    double rr = 0, bnorm;
-    if ((st = ad_dot(ctx, n, W->r, W->r, W, &rr))) {
-        free(h_a);
-        return st;
-    }
-    bnorm = sqrt(rr);
+    double rr = 0, bnorm = 0;
     int it = 0;
-    while (bnorm > 0 && sqrt(rr) > tol * bnorm && it < max_it) {
+    // b = P^T g = g - B X c (into r), the right-hand side of the projected system;
+    // CG on P^T (A - lambda B) P y = b from y = 0
+    st = ad_v_minus_xc(ctx, n, m, BX, ldbx, W->c, W->r, W->r);
+    if (!st) st = gb_set_zero(ctx, W->y, (size_t)n);
+    if (!st) st = ad_axpby(ctx, n, 1.0, W->r, 0.0, W->p);
+    if (!st) st = ad_dot(ctx, n, W->r, W->r, W, &rr);
+    bnorm = sqrt(rr);
+    while (!st && bnorm > 0 && sqrt(rr) > tol * bnorm && it < max_it) {
         double pq;
         if ((st = ad_apply(ctx, A, B, n, m, X, ldx, lambda, W->p, W->q, W))) break;
         if ((st = ad_dot(ctx, n, W->p, W->q, W, &pq))) break;
         if (!(pq > 0)) break;                               // left the SPD complement: stop
         const double alpha = rr / pq;
-        if ((st = gb_axpby(ctx, n, 1, alpha, W->p, 1, 1.0, W->y, 1))) break;
-        if ((st = gb_axpby(ctx, n, 1, -alpha, W->q, 1, 1.0, W->r, 1))) break;
+        if ((st = ad_axpby(ctx, n, alpha, W->p, 1.0, W->y))) break;
+        if ((st = ad_axpby(ctx, n, -alpha, W->q, 1.0, W->r))) break;
         double rr2;
         if ((st = ad_dot(ctx, n, W->r, W->r, W, &rr2))) break;
         const double beta = rr2 / rr;
         rr = rr2;
-        if ((st = gb_axpby(ctx, n, 1, 1.0, W->r, 1, beta, W->p, 1))) break;
+        if ((st = ad_axpby(ctx, n, 1.0, W->r, beta, W->p))) break;
         ++it;
     }
     if (iters) *iters = it;
-    if (st) {
-        free(h_a);
-        return st;
-    }
     // mu = P y + X a
-    if (B) {
-        if (!(st = gb_spmm(ctx, B, W->y, 1, W->w, 1, 1, 1.0, nullptr, 0.0, nullptr)))
-            st = ad_project(ctx, n, m, X, ldx, X, ldx, W->y, W->w, W->t, W);
-    } else {
-        st = ad_project(ctx, n, m, X, ldx, X, ldx, W->y, W->y, W->t, W);
-    }
     if (!st) {
-        if (cudaMemcpyAsync(W->c, h_a, sizeof(double) * m, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
-            st = gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+        if (B) {
+            if (!(st = gb_spmm(ctx, B, W->y, 1, W->w, 1, 1, 1.0, nullptr, 0.0, nullptr)))
+                st = ad_project(ctx, n, m, X, ldx, X, ldx, W->y, W->w, W->t, W);
+        } else {
+            st = ad_project(ctx, n, m, X, ldx, X, ldx, W->y, W->y, W->t, W);
+        }
     }
-    if (!st) st = gb_lincomb(ctx, n, m, 1, X, ldx, W->c, m, 1.0, 1.0, W->t, 1, 0);
+    if (!st && cudaMemcpyAsync(W->c, h_a, sizeof(double) * m, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+        st = gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+    if (!st) st = ad_v_minus_xc(ctx, n, m, X, ldx, W->c, W->t, W->t);
     if (!st) st = gb_axpby(ctx, n, 1, 1.0, W->t, 1, 0.0, mu, ldmu);
     cudaStreamSynchronize(ctx->stream);
     free(h_a);
@@ -301,7 +416,8 @@ extern "C" int GCGE_GPU_EigvecAdjoint(const gcge_gpu_mat *A, const gcge_gpu_mat 
     double *base = nullptr;
     // sub-buffers start on 256-byte boundaries
     const size_t vn = ((size_t)n + 31) & ~(size_t)31, vm = ((size_t)m + 31) & ~(size_t)31;
-    const size_t nv = 7 * vn + vm + 32 + (B ? (((size_t)n * m + 31) & ~(size_t)31) : 0);
+    const size_t np = (((size_t)ctx->num_sms * AV_BLOCKS_PER_SM * (size_t)(m > 1 ? m : 1)) + 31) & ~(size_t)31;
+    const size_t nv = 7 * vn + vm + 32 + np + (B ? (((size_t)n * m + 31) & ~(size_t)31) : 0);
     if (cudaMalloc(&base, sizeof(double) * nv) != cudaSuccess) return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
     W.y = base;
     W.r = W.y + vn;
@@ -312,14 +428,20 @@ extern "C" int GCGE_GPU_EigvecAdjoint(const gcge_gpu_mat *A, const gcge_gpu_mat 
     W.w = W.u + vn;
     W.c = W.w + vn;
     W.dot = W.c + vm;
-    W.BX = B ? W.dot + 32 : nullptr;
+    W.part = W.dot + 32;
+    W.BX = B ? W.part + np : nullptr;
     W.h_c = (double *)malloc(sizeof(double) * m);
     if (!W.h_c) {
         cudaFree(base);
         return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
     }
+    // the projections are n x m by one column: FP64-pipe Gram and combination
+    // kernels (no tensor-core set-up per call)
+    const int tc = ctx->tc;
+    ctx->tc = 0;
     st = ad_solve(ctx, A, B, n, m, X->d, X->ld, eval, k, G->d + g_col, G->ld, MU->d + mu_col, MU->ld, cluster_tol,
                   tol, max_it, iters, &W);
+    ctx->tc = tc;
     cudaStreamSynchronize(ctx->stream);
     cudaFree(base);
     free(W.h_c);

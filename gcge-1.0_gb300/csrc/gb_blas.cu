@@ -293,7 +293,9 @@ extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X
     ctx->spmm_launches++;
     GB_PROF(ctx, GB_K_SPMM64, 12.0 * A->nnz + 4.0 * (A->n + 1) + (beta != 0.0 ? 24.0 : 16.0) * A->n * k,
             2.0 * A->nnz * k);
-    if (k == 1) {
+    // one column: a warp per row for long rows; short rows (stencils) go to the
+    // lane-group kernel, 4 lanes per row
+    if (k == 1 && (double)A->nnz > 16.0 * A->n) {
         int grid = ceil_div_l((long)A->n * 32, 256);
         GB_LAUNCH(ctx, (k_spmv<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
                   Y, ldy, alpha, alpha_col, beta, ncols_dev);
