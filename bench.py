@@ -382,6 +382,8 @@ def run_kernel(args):
     rng = np.random.default_rng(0)
     if args.kernel == "adjoint":
         return run_adjoint(args, ctx)
+    if args.kernel in ("c3", "c5"):
+        return run_config(args, ctx)
     if args.kernel.startswith("spmm"):
         A, B = P.fem_q1_cube(args.ne)
         Msp = A if args.kernel == "spmm_a" else B
@@ -417,6 +419,48 @@ def run_kernel(args):
     ctx.close()
     print(json.dumps({"kernel": args.kernel, "shape": desc, "ms_per_call": dt * 1e3,
                       "fp64_equiv_tflops": flops / dt / 1e12 if dt > 0 else None}))
+
+
+def run_config(args, ctx):
+    """One mixed-precision solve of a large parity configuration, timed on the device,
+    with every residual checked on the host: c3 = 7-point variable-coefficient
+    diffusion on --nc^3 cells (sigma-1 Gaussian field, correlation length 8 cells,
+    lumped diagonal mass U[1, 2]), nev 100, block 128; c5 = weighted power-law
+    graph Laplacian + 1e-3 I on --n nodes, B = diag U[1, 2], nev 200, block 256,
+    plus the gradient of the eigenvalue sum with respect to diag(B)."""
+    import numpy as np
+    import gcge_gb300 as G
+    from gcge_gb300 import problems as P
+    t0 = time.time()
+    if args.kernel == "c3":
+        A, B = P.varcoef3d(nc=args.nc)
+        nev, block = 100, 128
+        desc = "varcoef3d %d^3" % args.nc
+    else:
+        A, B = P.powerlaw_graph(n=args.n)
+        nev, block = 200, 256
+        desc = "power-law graph n=%d" % args.n
+    gen_s = time.time() - t0
+    dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
+    X = ctx.multivec(A.n, nev)
+    params = ctx.params(nev=nev, block_size=block, ev_tol=1e-8, conv_type="BR", ev_max_it=args.max_it,
+                        seed=20241203, precision=1)
+    ev, Xh, st = ctx.solve(dA, dB, params, evec=X)
+    As, Bs = A.to_scipy(), B.to_scipy()
+    res = np.linalg.norm(As @ Xh - (Bs @ Xh) * ev[None, :], axis=0) / (np.abs(ev) * np.linalg.norm(Bs @ Xh, axis=0))
+    out = {"kernel": args.kernel, "shape": "%s: n=%d nnz(A)=%d, nev=%d, block=%d" % (desc, A.n, A.nnz, nev, block),
+           "problem_generation_s": gen_s, "solve_s": st.solve_ms * 1e-3, "iterations": st.num_iter,
+           "unconverged": st.num_unlock, "max_residual": float(res.max()), "lambda_min": float(ev[0]),
+           "lambda_max": float(ev[-1]), "phase_ms": st.as_dict()["phase_ms"]}
+    if args.kernel == "c5":
+        ctx.sync()
+        t = time.perf_counter()
+        gB = G.pattern_grad(dB, X, 0, X, 0, nev, -ev, len(B.val))
+        out["grad_sum_eig_wrt_diagB_s"] = time.perf_counter() - t
+        ref = -np.einsum("ij,ij,j->i", Xh, Xh, ev)
+        out["grad_max_rel_err"] = float(np.max(np.abs(gB - ref)) / np.max(np.abs(ref)))
+    ctx.close()
+    print(json.dumps(out))
 
 
 def run_adjoint(args, ctx):
@@ -468,13 +512,17 @@ def main():
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "bcg32", "lincomb", "gram", "adjoint"],
+    ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "bcg32", "lincomb", "gram", "adjoint", "c3", "c5"],
                     help="time one hot operation instead of the solve (profiling)")
-    ap.add_argument("--n", type=int, default=262144, help="rows for --kernel lincomb/gram")
+    ap.add_argument("--n", type=int, default=None, help="rows for --kernel lincomb/gram (262144) / nodes for c5 (2e6)")
     ap.add_argument("--ne", type=int, default=64, help="cube edge for --kernel spmm_a/spmm_b")
     ap.add_argument("--k", type=int, default=64, help="columns for --kernel spmm_a/spmm_b/bcg32")
-    ap.add_argument("--nc", type=int, default=512, help="cells per edge for --kernel adjoint")
+    ap.add_argument("--nc", type=int, default=None, help="cells per edge for --kernel adjoint (512) / c3 (160)")
     args = ap.parse_args()
+    if args.nc is None:
+        args.nc = 160 if args.kernel == "c3" else 512
+    if args.n is None:
+        args.n = 2_000_000 if args.kernel == "c5" else 262144
     if args.kernel:
         run_kernel(args)
         return

@@ -192,6 +192,21 @@ def test_small_nev_and_blocks(ctx, nev, bs):
     assert np.max(np.abs(ev - ex) / ex) < 1e-10
 
 
+def test_varcoef3d_mixed(ctx, oracle):
+    """7-point variable-coefficient diffusion (exp of a sigma-1 Gaussian field, lumped
+    diagonal mass U[1, 2]): the family of the 160^3 configuration at 16^3 cells."""
+    A, B = P.varcoef3d(nc=16)
+    dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
+    ev, X, st = ctx.solve(dA, dB, ctx.params(nev=20, block_size=24, seed=8, conv_type="BR", ev_max_it=500,
+                                             precision=1))
+    assert st.num_unlock == 0
+    oe, oX, ost = oracle.solve(A, B, oracle.params(nev=24, conv_type="BR", ev_tol=1e-11, ev_max_it=800,
+                                                   init_rng=1, seed=4))
+    assert ost.num_unlock == 0
+    assert np.max(np.abs(ev - oe[:20]) / np.abs(oe[:20])) < 1e-9
+    assert np.all(residuals(A, B, ev, X, "BR") <= 1.05e-8)
+
+
 def test_irregular_graph_mixed(ctx, oracle):
     """Power-law graph Laplacian (irregular rows up to 300 nonzeros), B = diag U[1,2]."""
     A, B = P.powerlaw_graph(4000, seed=11, dmax=300)
