@@ -581,7 +581,10 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
     const int quarter = warp & 3, col0 = (warp >> 2) * TC_COLS_PER_WARP;
     const int my_row = quarter * 32 + lane;
     const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + col0;
+    // alpha = +-1, beta = 0: the output is the drained value with its sign bit
+    // flipped or not, an integer operation (the FP64 pipe runs at 1/64 rate)
     const bool plain = beta == 0.0 && (alpha == 1.0 || alpha == -1.0);
+    const unsigned long long sflip = alpha == -1.0 ? 0x8000000000000000ull : 0ull;
     int commits[3] = {0, 0, 0};
     int copies[2] = {0, 0};                              // bulk copies per buffer (thread 0)
 
@@ -726,7 +729,10 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
                             const int j = j0 + col0 + g4 * 4 + q;
                             if (last && r < n && j < k2) {
                                 double *y = Y + r * ldy + j;
-                                *y = plain ? (alpha == 1.0 ? v2 : -v2) : fma(beta, *y, alpha * v2);
+                                if (plain)
+                                    *y = __longlong_as_double(__double_as_longlong(v2) ^ (long long)sflip);
+                                else
+                                    *y = fma(beta, *y, alpha * v2);
                             }
                         }
                     }
