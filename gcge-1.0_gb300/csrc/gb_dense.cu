@@ -17,6 +17,7 @@
 //    warp), inverse iteration with reorthogonalisation inside clusters of close
 //    eigenvalues, and back-transformation by the stored reflectors.
 #include <cfloat>
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "gb_internal.h"
@@ -266,7 +267,7 @@ extern "C" int gb_chol_deflate(gcge_gpu_ctx *ctx, int k, const double *G, int ld
 // work layout (doubles): Aw[m*m] | d[m] | e[m] | tau[m] | Zt[m*m] | lu[6*m*m] | scal[16]
 extern "C" size_t gb_syevx_work_doubles(int m)
 {
-    return (size_t)m * m * 8 + 3 * (size_t)m + 64;
+    return (size_t)m * m * 2 + 3 * (size_t)m + 64;     // Aw (m x m), d, e, tau, Zt (m x m)
 }
 
 // Householder reduction of the full symmetric H (lower reflectors, LAPACK dsytd2 "L").
@@ -370,6 +371,279 @@ k_tridiag(int m, const double *__restrict__ H, int ldh, double *__restrict__ Aw,
     }
 }
 
+// ---------------------------------------------------------------- cluster tridiagonalisation
+// The same reduction as k_tridiag (dsytd2 "L": reflectors in the columns of Aw,
+// d, e, tau) spread over a thread-block cluster of TC CTAs, so that the FP64 work
+// of the matrix-vector product and the rank-2 update runs on TC SMs. The lower
+// triangle is dealt out by columns, cyclically: column c lives in CTA c mod TC,
+// rows c..m-1, packed in that CTA's shared memory. Step i:
+//   A  the owner of column i forms the reflector (v, tau, beta) and publishes v;
+//   B  after a cluster barrier every CTA copies v (distributed shared memory) and
+//      forms its partial of p = A22 v from its own columns (row sums over the
+//      columns it holds left of the row, plus the column dots below the diagonal);
+//   C  after a second barrier every CTA adds the TC partials in rank order (the
+//      same sum everywhere), K = tau/2 p.v, w = tau p - K v, and updates its
+//      columns: A22 -= v w^T + w v^T.
+// Exchange buffers alternate by step parity; barriers are the hardware cluster
+// barrier (no waits on flags). All control flow is uniform over the cluster.
+#define TD_THREADS 512
+
+__device__ __forceinline__ double td_block_sum(double s, double *red)
+{
+    // fixed-order tree over the warps of the block (red: >= 32 doubles)
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+    if (lane == 0) red[w] = s;
+    __syncthreads();
+    if (w == 0) {
+        double t = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    const double r = red[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(TD_THREADS)
+k_tridiag_cluster(int m, const double *__restrict__ H, int ldh, double *__restrict__ Aw, double *__restrict__ d,
+                  double *__restrict__ e, double *__restrict__ tau)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int TC = (int)cl.num_blocks(), b = (int)cl.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = TD_THREADS >> 5;
+    extern __shared__ double tsm[];
+    __shared__ double red[33];
+    __shared__ double s_tau, s_scale;
+    const int ncol = b < m ? (m - 1 - b) / TC + 1 : 0;       // own columns b, b + TC, ...
+    // layout: vbuf[2][m], pbuf[2][m], v[m], p[m], then the packed columns; offsets int[ncol+1] after
+    double *vbuf = tsm, *pbuf = vbuf + 2 * (size_t)m, *v = pbuf + 2 * (size_t)m, *p = v + m, *A = p + m;
+    long tot = 0;
+    for (int l = 0; l < ncol; ++l) tot += m - (b + l * TC);
+    int *off = (int *)(A + tot);
+    if (tid == 0) {
+        int o = 0;
+        for (int l = 0; l < ncol; ++l) {
+            off[l] = o;
+            o += m - (b + l * TC);
+        }
+        off[ncol] = o;
+    }
+    __syncthreads();
+    for (int l = 0; l < ncol; ++l) {
+        const int c = b + l * TC;
+        for (int r = c + tid; r < m; r += TD_THREADS) A[off[l] + (r - c)] = H[r + (long)c * ldh];
+    }
+    __syncthreads();
+    for (int i = 0; i + 2 < m; ++i) {
+        const int len = m - i - 1, par = i & 1, owner = i % TC;
+        double *vb = vbuf + (size_t)par * m, *pb = pbuf + (size_t)par * m;
+        // ---- A: the owner forms the reflector of column i
+        if (b == owner) {
+            const int l = i / TC;
+            const double *col = A + off[l];               // rows i..m-1; x = rows i+1..
+            double sq = 0;
+            for (int r = 2 + tid; r <= len; r += TD_THREADS) sq = fma(col[r], col[r], sq);
+            const double xn2 = td_block_sum(sq, red);
+            if (tid == 0) {
+                const double alpha = col[1];
+                d[i] = col[0];
+                if (xn2 == 0.0) {
+                    s_tau = 0.0;
+                    e[i] = alpha;
+                    s_scale = 0.0;
+                } else {
+                    const double beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+                    s_tau = (beta - alpha) / beta;
+                    s_scale = 1.0 / (alpha - beta);
+                    e[i] = beta;
+                }
+                tau[i] = s_tau;
+            }
+            __syncthreads();
+            const double sc = s_scale;
+            for (int r = tid; r < len; r += TD_THREADS) {
+                const double vr = r == 0 ? 1.0 : col[1 + r] * sc;
+                vb[r] = vr;
+                if (r > 0) Aw[(long)i * m + i + 1 + r] = vr;      // stored reflector (unit lead implied)
+            }
+            if (tid == 0) vb[m - 1] = s_tau;                    // tau rides along in the last slot
+        }
+        cl.sync();
+        // ---- B: copy v and tau, partial p = A22 v over the own columns
+        const double *vr_own = cl.map_shared_rank(vbuf + (size_t)par * m, owner);
+        for (int r = tid; r < len; r += TD_THREADS) v[r] = vr_own[r];
+        if (tid == 0) s_tau = vr_own[m - 1];
+        __syncthreads();
+        const double tv = s_tau;
+        if (tv != 0.0) {
+            int l0 = (i + 1 - b + TC - 1) / TC;                  // first own column >= i + 1
+            if (i + 1 <= b) l0 = 0;
+            // row sums: p_b[r] = sum over own columns c <= row of A[row, c] v[c]
+            for (int r = tid; r < len; r += TD_THREADS) {
+                const int row = i + 1 + r;
+                double a0 = 0, a1 = 0;
+                int l = l0;
+                for (; l + 1 < ncol && b + (l + 1) * TC <= row; l += 2) {
+                    const int c0 = b + l * TC, c1 = c0 + TC;
+                    a0 = fma(A[off[l] + (row - c0)], v[c0 - i - 1], a0);
+                    a1 = fma(A[off[l + 1] + (row - c1)], v[c1 - i - 1], a1);
+                }
+                if (l < ncol && b + l * TC <= row) {
+                    const int c0 = b + l * TC;
+                    a0 = fma(A[off[l] + (row - c0)], v[c0 - i - 1], a0);
+                }
+                pb[r] = a0 + a1;
+            }
+            __syncthreads();
+            // column dots below the diagonal: p_b[c] += sum_{row > c} A[row, c] v[row]
+            for (int l = l0 + wid; l < ncol; l += nw) {
+                const int c = b + l * TC;
+                const double *col = A + off[l];
+                double s = 0;
+                for (int rr = 1 + lane; rr < m - c; rr += 32) s = fma(col[rr], v[c + rr - i - 1], s);
+#pragma unroll
+                for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+                if (lane == 0) pb[c - i - 1] += s;
+            }
+        }
+        cl.sync();
+        // ---- C: p = tau * sum of the partials (rank order), K, w, rank-2 update
+        if (tv != 0.0) {
+            for (int r = tid; r < len; r += TD_THREADS) {
+                double s = 0;
+                for (int q = 0; q < TC; ++q) s += cl.map_shared_rank(pbuf + (size_t)par * m, q)[r];
+                p[r] = tv * s;
+            }
+            __syncthreads();
+            double kv = 0;
+            for (int r = tid; r < len; r += TD_THREADS) kv = fma(p[r], v[r], kv);
+            const double K = 0.5 * tv * td_block_sum(kv, red);
+            for (int r = tid; r < len; r += TD_THREADS) p[r] -= K * v[r];     // p now holds w
+            __syncthreads();
+            int l0 = (i + 1 - b + TC - 1) / TC;
+            if (i + 1 <= b) l0 = 0;
+            for (int l = l0; l < ncol; ++l) {
+                const int c = b + l * TC, cc = c - i - 1;
+                const double vc = v[cc], wc = p[cc];
+                double *col = A + off[l];
+                for (int rr = tid; rr < m - c; rr += TD_THREADS) {
+                    const int rv = cc + rr;
+                    col[rr] -= v[rv] * wc + p[rv] * vc;
+                }
+            }
+        } else if (b == owner) {
+            // zero reflector: nothing to apply; the stored column below the subdiagonal is zero
+            for (int r = 1 + tid; r < len; r += TD_THREADS) Aw[(long)i * m + i + 1 + r] = 0.0;
+        }
+        __syncthreads();
+    }
+    // the last two diagonal entries and the last off-diagonal
+    if (m >= 2 && b == (m - 2) % TC && tid == 0) {
+        const double *col = A + off[(m - 2) / TC];
+        d[m - 2] = col[0];
+        e[m - 2] = col[1];
+        tau[m - 2] = 0.0;
+    }
+    if (b == (m - 1) % TC && tid == 0) {
+        d[m - 1] = A[off[(m - 1) / TC]];
+        e[m - 1] = 0.0;
+        tau[m - 1] = 0.0;
+    }
+    cl.sync();                                        // no CTA leaves while others may read its buffers
+}
+
+// shared memory of k_tridiag_cluster for m and a cluster of tc CTAs (CTA 0 holds the most)
+static size_t td_cluster_smem(int m, int tc)
+{
+    const int ncol = (m - 1) / tc + 1;
+    size_t tot = 0;
+    for (int l = 0; l < ncol; ++l) tot += (size_t)(m - l * tc);
+    return sizeof(double) * (6 * (size_t)m + tot) + sizeof(int) * (ncol + 1) + 16;
+}
+
+// cluster size for m, 0 if the single-SM kernel is to be used
+// Each of the m - 2 steps carries several microseconds of dependent FP64 latency
+// (reductions, the sqrt/division of the reflector, two cluster barriers) whatever
+// the number of SMs, so the cluster pays only where a step's arithmetic on one
+// SM (3 len^2 / 2 FMAs at ~2 FP64 FMA per clock) outweighs that: measured at
+// m = 178 the cluster takes 1.58 ms against 1.47 ms on one SM; m >= 256 goes
+// to the cluster (at m = 720 one SM needs ~60 ms of FP64 issue per reduction).
+static int td_cluster_size(gcge_gpu_ctx *ctx, int m)
+{
+    if (m < 256) return 0;
+    static int cached_m = -1, cached_tc = 0;
+    if (m == cached_m) {
+        if (cached_tc &&
+            cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)td_cluster_smem(m, cached_tc)) != cudaSuccess)
+            return 0;
+        return cached_tc;
+    }
+    cached_m = m;
+    cached_tc = 0;
+    static int probed = 0, allow16 = 0;
+    if (!probed) {
+        probed = 1;
+        if (cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+            allow16 = 1;
+        cudaGetLastError();
+    }
+    const int want = m >= 256 && allow16 ? 16 : 8;
+    for (int tc = want; tc >= 8; tc /= 2) {
+        const size_t smem = td_cluster_smem(m, tc);
+        if (smem > 200 * 1024) continue;
+        if (cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = tc;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(tc);
+        cfg.blockDim = dim3(TD_THREADS);
+        cfg.dynamicSmemBytes = smem;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_tridiag_cluster, &cfg) == cudaSuccess && nclusters > 0)
+            return cached_tc = tc;
+        cudaGetLastError();
+    }
+    (void)ctx;
+    return 0;
+}
+
+static int td_cluster_launch(gcge_gpu_ctx *ctx, int tc, int m, const double *H, int ldh, double *Aw, double *d,
+                             double *e, double *tau)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = tc;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(tc);
+    cfg.blockDim = dim3(TD_THREADS);
+    cfg.dynamicSmemBytes = td_cluster_smem(m, tc);
+    cfg.stream = ctx->stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_tridiag_cluster, m, H, ldh, Aw, d, e, tau) != cudaSuccess)
+        return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+    ctx->launches++;
+    if (ctx->prof) gb_prof_end(ctx);
+    return gb_check_launch(ctx);
+}
+
 // number of eigenvalues of the tridiagonal (d, e2 = e^2) smaller than x (the
 // ratio form of the Sturm sequence with the pivmin guard; its count is monotone
 // in x under IEEE arithmetic, which the bisection relies on inside clusters)
@@ -459,12 +733,66 @@ __device__ __forceinline__ double start_value(int j, int i)
     return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
 }
 
-__global__ void k_invit(int m, const double *__restrict__ d, const double *__restrict__ e, int nev,
-                        const double *__restrict__ eval, double *__restrict__ Zt, int ldz, double *__restrict__ lu)
+// 1/x by Newton-Raphson refinement of the hardware reciprocal approximation
+// (rcp.approx.ftz.f64): two steps r <- r + r (1 - x r) square the relative error
+// each time, leaving a few ulp. For the pivots of inverse iteration, whose
+// iterate tolerates a slightly perturbed solve; an exact IEEE division costs
+// several hundred cycles on this chain. Tiny or zero x take the exact division.
+__device__ __forceinline__ double nr_recip(double x)
 {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nev) return;
-    double *dl = lu + (size_t)j * 6 * m, *dd = dl + m, *du = dd + m, *du2 = du + m, *inv = du2 + m, *ip = inv + m;
+    if (!(fabs(x) >= DBL_MIN) || isinf(x)) return 1.0 / x;
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double t = fma(-x, r, 1.0);
+    r = fma(r, t, r);
+    t = fma(-x, r, 1.0);
+    return fma(r, t, r);
+}
+
+__global__ void k_recip_probe(int n, const double *__restrict__ x, double *__restrict__ r)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = nr_recip(x[i]);
+}
+
+// Internal check of nr_recip (not part of the public interface): r[i] = nr_recip(x[i])
+// for n host values, on the current device.
+extern "C" int gb_recip_check(int n, const double *x_host, double *r_host)
+{
+    if (n <= 0 || !x_host || !r_host) return GCGE_GPU_ERR_ARG;
+    double *dx = nullptr, *dr = nullptr;
+    int st = GCGE_GPU_OK;
+    if (cudaMalloc(&dx, sizeof(double) * n) != cudaSuccess || cudaMalloc(&dr, sizeof(double) * n) != cudaSuccess ||
+        cudaMemcpy(dx, x_host, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+        st = GCGE_GPU_ERR_CUDA;
+    if (!st) {
+        k_recip_probe<<<(n + 255) / 256, 256>>>(n, dx, dr);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpy(r_host, dr, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = GCGE_GPU_ERR_CUDA;
+    }
+    cudaFree(dx);
+    cudaFree(dr);
+    return st;
+}
+
+// inverse iteration: one thread per wanted eigenvalue, IV per block (one warp);
+// LU of T - lambda I with partial pivoting (dgttrf layout) and three solves from
+// a hashed start vector. The working arrays of the block's eigenvalues sit in
+// shared memory, element i of lane l at [i * IV + l] (consecutive lanes,
+// consecutive words: no bank conflicts).
+__global__ void __launch_bounds__(32)
+k_invit(int m, const double *__restrict__ d, const double *__restrict__ e, int nev,
+        const double *__restrict__ eval, double *__restrict__ Zt, int ldz, int IV)
+{
+    extern __shared__ double ism[];
+    const int lane = threadIdx.x;
+    const int j = blockIdx.x * IV + lane;
+    if (lane >= IV || j >= nev) return;
+    double *dl = ism, *dd = dl + (size_t)m * IV, *du = dd + (size_t)m * IV, *du2 = du + (size_t)m * IV;
+    double *inv = du2 + (size_t)m * IV, *z = inv + (size_t)m * IV;
+    int *ip = (int *)(z + (size_t)m * IV);
+#define IX(i) ((size_t)(i) * IV + lane)
     double tnorm = 0;
     for (int i = 0; i < m; ++i)
         tnorm = fmax(tnorm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < m - 1 ? fabs(e[i]) : 0.0));
@@ -477,77 +805,93 @@ __global__ void k_invit(int m, const double *__restrict__ d, const double *__res
         lam = eval[k] + (double)(j - k) * pert;
     }
     for (int i = 0; i < m; ++i) {
-        dd[i] = d[i] - lam;
-        dl[i] = (i < m - 1) ? e[i] : 0.0;
-        du[i] = (i < m - 1) ? e[i] : 0.0;
-        du2[i] = 0.0;
-        ip[i] = (double)i;
+        dd[IX(i)] = d[i] - lam;
+        dl[IX(i)] = (i < m - 1) ? e[i] : 0.0;
+        du[IX(i)] = (i < m - 1) ? e[i] : 0.0;
+        du2[IX(i)] = 0.0;
+        ip[IX(i)] = i;
     }
     for (int i = 0; i + 1 < m; ++i) {
-        if (fabs(dd[i]) >= fabs(dl[i])) {
-            if (dd[i] != 0.0) {
-                const double f = dl[i] / dd[i];
-                dl[i] = f;
-                dd[i + 1] -= f * du[i];
+        const double di = dd[IX(i)], li = dl[IX(i)];
+        if (fabs(di) >= fabs(li)) {
+            if (di != 0.0) {
+                const double f = li * nr_recip(di);
+                dl[IX(i)] = f;
+                dd[IX(i + 1)] -= f * du[IX(i)];
             } else {
-                dl[i] = 0.0;
+                dl[IX(i)] = 0.0;
             }
         } else {
-            const double f = dd[i] / dl[i];
-            dd[i] = dl[i];
-            dl[i] = f;
-            const double t = du[i];
-            du[i] = dd[i + 1];
-            dd[i + 1] = t - f * dd[i + 1];
+            const double f = di * nr_recip(li);
+            dd[IX(i)] = li;
+            dl[IX(i)] = f;
+            const double t = du[IX(i)];
+            const double dn = dd[IX(i + 1)];
+            du[IX(i)] = dn;
+            dd[IX(i + 1)] = t - f * dn;
             if (i + 2 < m) {
-                du2[i] = du[i + 1];
-                du[i + 1] = -f * du[i + 1];
+                du2[IX(i)] = du[IX(i + 1)];
+                du[IX(i + 1)] = -f * du[IX(i + 1)];
             }
-            ip[i] = (double)(i + 1);
+            ip[IX(i)] = i + 1;
         }
     }
     const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
     for (int i = 0; i < m; ++i) {
-        if (fabs(dd[i]) < tiny) dd[i] = copysign(tiny, dd[i] == 0.0 ? 1.0 : dd[i]);
-        inv[i] = 1.0 / dd[i];
+        double di = dd[IX(i)];
+        if (fabs(di) < tiny) di = copysign(tiny, di == 0.0 ? 1.0 : di);
+        dd[IX(i)] = di;
+        inv[IX(i)] = nr_recip(di);
     }
-    double *z = Zt + (size_t)j * ldz;
-    for (int i = 0; i < m; ++i) z[i] = start_value(j, i);
+    for (int i = 0; i < m; ++i) z[IX(i)] = start_value(j, i);
     for (int iter = 0; iter < 3; ++iter) {
         // solve L U x = z (dgttrs, no transpose)
         for (int i = 0; i + 1 < m; ++i) {
-            if ((int)ip[i] == i) {
-                z[i + 1] -= dl[i] * z[i];
+            if (ip[IX(i)] == i) {
+                z[IX(i + 1)] -= dl[IX(i)] * z[IX(i)];
             } else {
-                const double t = z[i];
-                z[i] = z[i + 1];
-                z[i + 1] = t - dl[i] * z[i];
+                const double t = z[IX(i)];
+                z[IX(i)] = z[IX(i + 1)];
+                z[IX(i + 1)] = t - dl[IX(i)] * z[IX(i)];
             }
         }
-        z[m - 1] *= inv[m - 1];
-        if (m >= 2) z[m - 2] = (z[m - 2] - du[m - 2] * z[m - 1]) * inv[m - 2];
-        for (int i = m - 3; i >= 0; --i) z[i] = (z[i] - du[i] * z[i + 1] - du2[i] * z[i + 2]) * inv[i];
+        z[IX(m - 1)] *= inv[IX(m - 1)];
+        if (m >= 2) z[IX(m - 2)] = (z[IX(m - 2)] - du[IX(m - 2)] * z[IX(m - 1)]) * inv[IX(m - 2)];
+        for (int i = m - 3; i >= 0; --i)
+            z[IX(i)] = (z[IX(i)] - du[IX(i)] * z[IX(i + 1)] - du2[IX(i)] * z[IX(i + 2)]) * inv[IX(i)];
         double mx = 0;
-        for (int i = 0; i < m; ++i) mx = fmax(mx, fabs(z[i]));
-        const double s = mx > 0 ? 1.0 / mx : 1.0;
-        for (int i = 0; i < m; ++i) z[i] *= s;
+        for (int i = 0; i < m; ++i) mx = fmax(mx, fabs(z[IX(i)]));
+        const double sc = mx > 0 ? 1.0 / mx : 1.0;
+        for (int i = 0; i < m; ++i) z[IX(i)] *= sc;
     }
     double nn = 0;
-    for (int i = 0; i < m; ++i) nn = fma(z[i], z[i], nn);
-    const double s = 1.0 / sqrt(nn);
-    for (int i = 0; i < m; ++i) z[i] *= s;
+    for (int i = 0; i < m; ++i) nn = fma(z[IX(i)], z[IX(i)], nn);
+    const double sc = 1.0 / sqrt(nn);
+    double *zo = Zt + (size_t)j * ldz;
+    for (int i = 0; i < m; ++i) zo[i] = z[IX(i)] * sc;
+#undef IX
 }
 
 // reorthogonalise inside clusters (gap <= 1e-3 ||T||_1, as dstein) by two
-// classical Gram-Schmidt passes, then normalise. One block, vectors in order.
+// classical Gram-Schmidt passes, then normalise. One block, vectors in order;
+// with SMEM the nev vectors are worked on in shared memory (m * nev doubles).
+template <bool SMEM>
 __global__ void __launch_bounds__(1024)
 k_cluster_orth(int m, const double *__restrict__ d, const double *__restrict__ e, int nev,
-               const double *__restrict__ eval, double *__restrict__ Zt, int ldz)
+               const double *__restrict__ eval, double *__restrict__ Zg, int ldz)
 {
+    extern __shared__ double zsm[];
     __shared__ double coef[1024];
     __shared__ double s_tn;
     __shared__ double red[32];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    double *Zt = Zg;
+    long ld = ldz;
+    if (SMEM) {
+        for (long t = tid; t < (long)m * nev; t += blockDim.x) zsm[t] = Zg[(t / m) * ldz + t % m];
+        Zt = zsm;
+        ld = m;
+    }
     if (tid == 0) {
         double t = 0;
         for (int i = 0; i < m; ++i)
@@ -559,12 +903,12 @@ k_cluster_orth(int m, const double *__restrict__ d, const double *__restrict__ e
     int cs = 0;
     for (int j = 0; j < nev; ++j) {
         if (j > 0 && eval[j] - eval[j - 1] > ortol) cs = j;
-        double *zj = Zt + (size_t)j * ldz;
+        double *zj = Zt + (size_t)j * ld;
         const int np = j - cs;
         if (np > 0) {
             for (int pass = 0; pass < 2; ++pass) {
                 for (int q = wid; q < np; q += nw) {
-                    const double *zi = Zt + (size_t)(cs + q) * ldz;
+                    const double *zi = Zt + (size_t)(cs + q) * ld;
                     double s = 0;
                     for (int r = lane; r < m; r += 32) s = fma(zi[r], zj[r], s);
                     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
@@ -573,7 +917,7 @@ k_cluster_orth(int m, const double *__restrict__ d, const double *__restrict__ e
                 __syncthreads();
                 for (int r = tid; r < m; r += blockDim.x) {
                     double acc = zj[r];
-                    for (int q = 0; q < np && q < 1024; ++q) acc -= coef[q] * Zt[(size_t)(cs + q) * ldz + r];
+                    for (int q = 0; q < np && q < 1024; ++q) acc -= coef[q] * Zt[(size_t)(cs + q) * ld + r];
                     zj[r] = acc;
                 }
                 __syncthreads();
@@ -594,6 +938,8 @@ k_cluster_orth(int m, const double *__restrict__ d, const double *__restrict__ e
         for (int r = tid; r < m; r += blockDim.x) zj[r] *= inv;
         __syncthreads();
     }
+    if (SMEM)
+        for (long t = tid; t < (long)m * nev; t += blockDim.x) Zg[(t / m) * ldz + t % m] = zsm[t];
 }
 
 // Z = Q Zt with Q = H_0 H_1 ... H_{m-3}; one warp per column, reflectors in reverse.
@@ -633,19 +979,47 @@ extern "C" int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int 
     if (m <= 0 || il < 1 || iu > m || il > iu) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     if (m > 3000) return gb_fail(ctx, GCGE_GPU_ERR_ARG);   // dynamic shared memory of k_tridiag / k_bisect (2m doubles)
     const int nev = iu - il + 1;
-    double *Aw = work, *d = Aw + (size_t)m * m, *e = d + m, *tau = e + m, *Zt = tau + m, *lu = Zt + (size_t)m * m;
+    double *Aw = work, *d = Aw + (size_t)m * m, *e = d + m, *tau = e + m, *Zt = tau + m;
     if (cudaMemsetAsync(info_dev, 0, sizeof(int), ctx->stream) != cudaSuccess) return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
     const int tthreads = m >= 512 ? 1024 : (m >= 128 ? 512 : 256);
     GB_PROF(ctx, GB_K_EIG, 8.0 * m * m, 4.0 / 3.0 * m * (double)m * m);
-    GB_LAUNCH(ctx, k_tridiag, 1, tthreads, 2 * m * sizeof(double), m, H, ldh, Aw, d, e, tau);
+    const int tc = td_cluster_size(ctx, m);
+    if (tc) {
+        int st = td_cluster_launch(ctx, tc, m, H, ldh, Aw, d, e, tau);
+        if (st) return st;
+    } else {
+        GB_LAUNCH(ctx, k_tridiag, 1, tthreads, 2 * m * sizeof(double), m, H, ldh, Aw, d, e, tau);
+    }
     const int warps_per_block = 1;     // one eigenvalue per SM: the Sturm chains use the FP64 pipe
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
     GB_LAUNCH(ctx, k_bisect, (nev + warps_per_block - 1) / warps_per_block, 32 * warps_per_block,
               2 * m * sizeof(double), m, d, e, il, iu, eval, info_dev);
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
-    GB_LAUNCH(ctx, k_invit, (nev + 31) / 32, 32, 0, m, d, e, nev, eval, Zt, m, lu);
+    // inverse iteration: one eigenvalue per one-warp block, so that the chains spread
+    // over the SMs (the FP64 pipe of an SM is narrow: chains sharing one SM queue
+    // on it); working arrays in shared memory
+    const size_t per_eig = (size_t)m * (6 * sizeof(double) + sizeof(int));
+    const int IV = 1;
+    const size_t ismem = per_eig * IV;
+    // the 48 KB default covers static + dynamic shared memory together: both kernels
+    // are opened once to the most they can ask for (k_invit <= 156 KB at m = 3000,
+    // k_cluster_orth<true> <= 160 KB + its 8.3 KB static)
+    static bool attrs = false;
+    if (!attrs) {
+        if (cudaFuncSetAttribute(k_invit, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess ||
+            cudaFuncSetAttribute(k_cluster_orth<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) !=
+                cudaSuccess)
+            return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+        attrs = true;
+    }
+    GB_LAUNCH(ctx, k_invit, (nev + IV - 1) / IV, 32, ismem, m, d, e, nev, eval, Zt, m, IV);
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
-    GB_LAUNCH(ctx, k_cluster_orth, 1, 1024, 0, m, d, e, nev, eval, Zt, m);
+    const size_t osmem = sizeof(double) * (size_t)m * nev;
+    if (osmem <= 160 * 1024) {
+        GB_LAUNCH(ctx, k_cluster_orth<true>, 1, 1024, osmem, m, d, e, nev, eval, Zt, m);
+    } else {
+        GB_LAUNCH(ctx, k_cluster_orth<false>, 1, 1024, 0, m, d, e, nev, eval, Zt, m);
+    }
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
     GB_LAUNCH(ctx, k_backtransform, (nev * 32 + 255) / 256, 256, 0, m, Aw, tau, nev, Zt, m, Z, ldz);
     GB_LAUNCH(ctx, k_check_finite, 64, 256, 0, m, nev, Z, ldz, info_dev);

@@ -165,6 +165,29 @@ def test_bcg_fp32_tracks_fp64_while_columns_deactivate(ctx, k, max_it, rate):
     assert rel(out[1], out[0]) < 1e-4
 
 
+def test_newton_reciprocal_of_inverse_iteration(ctx):
+    """The reciprocal used for the pivots of inverse iteration (hardware
+    approximation refined by two Newton-Raphson steps) is within 2 ulp of the
+    IEEE quotient 1/x over the normal range; zero, infinities and subnormal
+    inputs take the exact division."""
+    import ctypes as C
+    lib = G.load()
+    rng = np.random.default_rng(12)
+    x = np.concatenate([rng.uniform(1.0, 2.0, 4000) * np.exp2(rng.integers(-1020, 1020, 4000)),
+                        -rng.uniform(1.0, 2.0, 1000) * np.exp2(rng.integers(-60, 60, 1000)),
+                        [1.0, -1.0, 3.0, 2.0 ** -1022, 2.0 ** 1023, 0.0, -0.0, np.inf, -np.inf, 5e-324, 1e-310]])
+    r = np.zeros_like(x)
+    lib.gb_recip_check.restype = C.c_int
+    assert lib.gb_recip_check(len(x), x.ctypes.data_as(C.c_void_p), r.ctypes.data_as(C.c_void_p)) == 0
+    with np.errstate(divide="ignore", over="ignore"):
+        ref = 1.0 / x
+    normal = np.isfinite(ref) & (np.abs(x) >= 2.0 ** -1022) & np.isfinite(x) & (np.abs(ref) >= 2.0 ** -1022)
+    ulp = np.spacing(np.abs(ref[normal]))
+    assert np.max(np.abs(r[normal] - ref[normal]) / ulp) <= 2.0
+    special = ~normal
+    assert np.array_equal(r[special], ref[special]) or np.allclose(r[special], ref[special], rtol=1e-15, equal_nan=True)
+
+
 @pytest.mark.parametrize("use_b", [False, True])
 def test_orthonormalize(ctx, use_b):
     Aa, Bb = P.fem_q1_cube(12)

@@ -151,10 +151,11 @@ def test_table_members_against_oracle(env):
     assert ctx.last_error() == 0
 
 
-def test_table_dense_eigensolver_matches_lapack(env):
+@pytest.mark.parametrize("m", [57, 130, 300, 520])   # one SM (m < 256); the cluster tridiagonalisation
+def test_table_dense_eigensolver_matches_lapack(env, m):
     ctx, tab = env
-    rng = np.random.default_rng(12)
-    m, lda = 57, 60
+    rng = np.random.default_rng(12 + m)
+    lda = m + 3
     M = rng.standard_normal((m, m))
     M = M + M.T
     M[20, 21] = M[21, 20] = 0.0
@@ -163,13 +164,14 @@ def test_table_dense_eigensolver_matches_lapack(env):
     il, iu = 1, 12
     k = iu - il + 1
     ev = np.zeros(m)
-    Z = np.zeros((k, 64))           # lde = 64
+    lde = m + 7
+    Z = np.zeros((k, lde))
     nev, info = C.c_int(), C.c_int()
     iv = lambda v: C.byref(C.c_int(v))  # noqa: E731
     dummy = C.c_double()
     tab.DenseMatEigenSolver(b"V", b"I", b"U", iv(m), a.ctypes.data_as(PD), iv(lda), C.byref(dummy),
                             C.byref(dummy), iv(il), iv(iu), C.byref(dummy), C.byref(nev), ev.ctypes.data_as(PD),
-                            Z.ctypes.data_as(PD), iv(64), None, None, iv(8 * m), None, None, None, C.byref(info))
+                            Z.ctypes.data_as(PD), iv(lde), None, None, iv(8 * m), None, None, None, C.byref(info))
     assert info.value == 0 and nev.value == k
     w, U = sl.eigh(M)
     np.testing.assert_allclose(ev[:k], w[:k], rtol=1e-12, atol=1e-12 * np.abs(w).max())
