@@ -343,6 +343,13 @@ extern "C" int GCGE_GPU_MatSetValues(gcge_gpu_mat *A, const double *val)
     gcge_gpu_ctx *ctx = A->ctx;
     if (!A->nnz) return GCGE_GPU_OK;
     CUDA_TRY(ctx, cudaMemcpyAsync(A->v, val, sizeof(double) * A->nnz, cudaMemcpyHostToDevice, ctx->stream));
+    if (A->dinv) {                         // the Jacobi diagonal follows the values
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(A->dinv);
+        cudaFree(A->dinv32);
+        A->dinv = nullptr;
+        A->dinv32 = nullptr;
+    }
     if (A->v32) {
         k_d2f_vals<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(A->nnz, A->v, A->v32);
         ctx->launches++;
@@ -360,6 +367,8 @@ extern "C" int GCGE_GPU_MatDestroy(gcge_gpu_mat *A)
     if (A->ci) cudaFree(A->ci);
     if (A->v) cudaFree(A->v);
     if (A->v32) cudaFree(A->v32);
+    if (A->dinv) cudaFree(A->dinv);
+    if (A->dinv32) cudaFree(A->dinv32);
     free(A);
     return GCGE_GPU_OK;
 }

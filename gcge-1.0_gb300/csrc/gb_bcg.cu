@@ -53,7 +53,8 @@ struct bcg_state {
 // beta[c] = rho2[c] / rho1[c] was formed once per column by k_finalize
 template <typename T>
 __global__ void k_pupdate(int n, int k, const T *__restrict__ R, T *__restrict__ P, long ld,
-                          const double *__restrict__ beta, const int *__restrict__ nact, int first)
+                          const double *__restrict__ beta, const int *__restrict__ nact, int first,
+                          const T *__restrict__ dinv)
 {
     const int ka = min(*nact, k);
     if (ka <= 0) return;
@@ -62,7 +63,8 @@ __global__ void k_pupdate(int n, int k, const T *__restrict__ R, T *__restrict__
     {
         const T *rr = R + r * ld;
         T *pr = P + r * ld;
-        for (int c = lane; c < ka; c += 32) pr[c] = first ? rr[c] : rr[c] + (T)beta[c] * pr[c];
+        const T dr = dinv ? dinv[r] : (T)1;                // z = D^-1 r (Jacobi) or r
+        for (int c = lane; c < ka; c += 32) pr[c] = first ? dr * rr[c] : dr * rr[c] + (T)beta[c] * pr[c];
     }
 }
 
@@ -70,7 +72,7 @@ __global__ void k_pupdate(int n, int k, const T *__restrict__ R, T *__restrict__
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_dot_partial(int n, int k, const T *__restrict__ A, const T *__restrict__ B, long ld,
-              const int *__restrict__ nact, double *__restrict__ part)
+              const int *__restrict__ nact, double *__restrict__ part, const T *__restrict__ wdiag = nullptr)
 {
     __shared__ double sh[8][33];
     const int ka = nact ? *nact : k;
@@ -84,7 +86,7 @@ k_dot_partial(int n, int k, const T *__restrict__ A, const T *__restrict__ B, lo
             T run = 0;
 #pragma unroll
             for (int q = 0; q < 8; ++q, r += 8)
-                if (r < r1) run = fma(A[r * ld + c], B[r * ld + c], run);
+                if (r < r1) run = fma(A[r * ld + c], wdiag ? wdiag[r] * B[r * ld + c] : B[r * ld + c], run);
             s += (double)run;
         }
     }
@@ -103,7 +105,7 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 k_xr_update(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restrict__ P,
             const T *__restrict__ W, long ld, const double *__restrict__ alpha,
-            const int *__restrict__ nact, double *__restrict__ part)
+            const int *__restrict__ nact, double *__restrict__ part, const T *__restrict__ dinv)
 {
     __shared__ double sh[8][33];
     const int ka = *nact;
@@ -123,7 +125,7 @@ k_xr_update(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restr
                     X[o] = X[o] + a * P[o];
                     const T rn = R[o] - a * W[o];
                     R[o] = rn;
-                    run = fma(rn, rn, run);
+                    run = fma(rn, dinv ? dinv[r] * rn : rn, run);   // r.z, z = D^-1 r or r
                 }
             }
             s += (double)run;
@@ -275,7 +277,8 @@ __device__ __forceinline__ void vb_block_reduce(const double s[4], int slot, int
 template <int TPR>
 __global__ void __launch_bounds__(VB_THREADS)
 k_pupdate_v(int n, int k, const float *__restrict__ R, float *__restrict__ P, long ld,
-            const double *__restrict__ beta, const int *__restrict__ nact, int first)
+            const double *__restrict__ beta, const int *__restrict__ nact, int first,
+            const float *__restrict__ dinv)
 {
     constexpr int RPB = VB_THREADS / TPR;
     const int ka = min(*nact, k);
@@ -287,7 +290,11 @@ k_pupdate_v(int n, int k, const float *__restrict__ R, float *__restrict__ P, lo
     for (int q = 0; q < 4; ++q) b[q] = (!first && c0 + q < ka) ? (float)beta[c0 + q] : 0.f;
     const bool full = c0 + 4 <= ka;
     for (long r = (long)blockIdx.x * RPB + rs; r < n; r += (long)gridDim.x * RPB) {
-        const float4 rv = *reinterpret_cast<const float4 *>(R + r * ld + c0);
+        float4 rv = *reinterpret_cast<const float4 *>(R + r * ld + c0);
+        if (dinv) {                                // z = D^-1 r (Jacobi)
+            const float dr = dinv[r];
+            rv.x *= dr; rv.y *= dr; rv.z *= dr; rv.w *= dr;
+        }
         float4 *pp = reinterpret_cast<float4 *>(P + r * ld + c0);
         if (first) {                               // p = r: the old p (uninitialised) is not read
             if (full) {
@@ -322,7 +329,7 @@ template <int TPR>
 __global__ void __launch_bounds__(VB_THREADS)
 k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const float *__restrict__ P,
               const float *__restrict__ W, long ld, const double *__restrict__ alpha, const int *__restrict__ nact,
-              double *__restrict__ part)
+              double *__restrict__ part, const float *__restrict__ dinv)
 {
     constexpr int RPB = VB_THREADS / TPR;
     const int ka = min(*nact, k);
@@ -343,11 +350,12 @@ k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const 
             const float4 wv = *reinterpret_cast<const float4 *>(W + o);
             float *xe = &xv.x, *re = &rv.x;
             const float *pe = &pv.x, *we = &wv.x;
+            const float dr = dinv ? dinv[r] : 1.0f;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 xe[q] = xe[q] + a[q] * pe[q];      // a = 0 leaves inactive columns unchanged
                 re[q] = re[q] - a[q] * we[q];
-                run[q] = fmaf(re[q], re[q], run[q]);
+                run[q] = fmaf(re[q], dr * re[q], run[q]);   // r.z, z = D^-1 r or r
             }
             *reinterpret_cast<float4 *>(X + o) = xv;
             *reinterpret_cast<float4 *>(R + o) = rv;
@@ -519,11 +527,12 @@ k_colsum_finalize(int nblk, int k, const double *__restrict__ part, double *sums
     if (threadIdx.x == 0) *nact = cnt;
 }
 
-typedef void (*pupdate_fn)(int, int, const float *, float *, long, const double *, const int *, int);
+typedef void (*pupdate_fn)(int, int, const float *, float *, long, const double *, const int *, int,
+                           const float *);
 typedef void (*spmm32_fn)(int, const int *, const int *, const float *, const float *, float *, long, int,
                           const int *, double *);
 typedef void (*xr_fn)(int, int, float *, float *, const float *, const float *, long, const double *, const int *,
-                      double *);
+                      double *, const float *);
 
 static int bcg_rounds32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, float *R, float *X, float *P, float *W, long ld,
                         const gb_bcg_args *a, bcg_state *s)
@@ -545,13 +554,14 @@ static int bcg_rounds32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, float *R, floa
     const int Gx = vec_blocks(ctx, (const void *)xru, n, ctiles);
     for (int it = 1; it < a->max_it; ++it) {
         GB_PROF(ctx, GB_K_BCGVEC, 12.0 * n * k, 2.0 * n * k);
-        GB_LAUNCH(ctx, pup, dim3(Gp, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
+        GB_LAUNCH(ctx, pup, dim3(Gp, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1, a->dinv32);
         ctx->spmm_launches++;
         GB_PROF(ctx, GB_K_SPMM32, 8.0 * A->nnz + 4.0 * (A->n + 1) + 12.0 * A->n * k, 2.0 * A->nnz * k + 2.0 * A->n * k);
         GB_LAUNCH(ctx, spm, Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
         GB_LAUNCH(ctx, k_colsum_alpha, k, 256, 0, Gs, k, s->part, s->nact, s->rho2, s->ptw, s->alpha);
         GB_PROF(ctx, GB_K_BCGVEC, 24.0 * n * k, 6.0 * n * k);
-        GB_LAUNCH(ctx, xru, dim3(Gx, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part);
+        GB_LAUNCH(ctx, xru, dim3(Gx, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part,
+                  a->dinv32);
         GB_LAUNCH(ctx, k_colsum_finalize, 1, 1024, 0, Gx, k, s->part, s->sums, s->rho1, s->rho2, s->err, s->nact,
                   a->rate, s->beta);
     }
@@ -565,9 +575,10 @@ static int bcg_rounds(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, T *R, T *X, T *P
     const int n = a->n, k = a->k, nblk = cdiv(n > 0 ? n : 1, RED_ROWS);
     dim3 rgrid(nblk, (k + 31) / 32);
     const double es = sizeof(T);
+    const T *dv = sizeof(T) == sizeof(double) ? (const T *)(const void *)a->dinv : (const T *)(const void *)a->dinv32;
     for (int it = 1; it < a->max_it; ++it) {
         GB_PROF(ctx, GB_K_BCGVEC, 3.0 * es * n * k, 2.0 * n * k);
-        GB_LAUNCH(ctx, k_pupdate<T>, row_grid(ctx, n), 256, 0, n, k, R, P, ld, s->beta, s->nact, it == 1);
+        GB_LAUNCH(ctx, k_pupdate<T>, row_grid(ctx, n), 256, 0, n, k, R, P, ld, s->beta, s->nact, it == 1, dv);
         int st;
         if (sizeof(T) == sizeof(double))
             st = gb_spmm(ctx, A, (const double *)P, ld, (double *)W, ld, k, 1.0, nullptr, 0.0, s->nact);
@@ -579,7 +590,7 @@ static int bcg_rounds(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, T *R, T *X, T *P
         GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s->part, s->nact, s->ptw);
         GB_LAUNCH(ctx, k_sum_active, (k + 127) / 128, 128, 0, k, s->nact, s->ptw, s->rho2, s->alpha);
         GB_PROF(ctx, GB_K_BCGVEC, 6.0 * es * n * k, 6.0 * n * k);
-        GB_LAUNCH(ctx, k_xr_update<T>, rgrid, 256, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part);
+        GB_LAUNCH(ctx, k_xr_update<T>, rgrid, 256, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part, dv);
         GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s->part, s->nact, s->sums);
         GB_LAUNCH(ctx, k_finalize, 1, 256, 0, k, s->sums, s->rho1, s->rho2, s->err, s->nact, a->rate, s->beta);
     }
@@ -618,7 +629,8 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
         if (st) return st;
         // P and W use the compact ld; R and X keep their own ld through the copies below
         if (ldr == ld && ldx == ld) {
-            GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, RHS, RHS, ld, (const int *)nullptr, s.part);
+            GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, RHS, RHS, ld, (const int *)nullptr, s.part,
+                      a->dinv);
             GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
             GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
             return bcg_rounds<double>(ctx, A, RHS, X, P, W, ld, a, &s);
@@ -629,7 +641,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
         if ((size_t)(w - (char *)work) > work_bytes) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
         if ((st = gb_axpby(ctx, n, k, 1.0, RHS, ldr, 0.0, R, ld))) return st;
         if ((st = gb_axpby(ctx, n, k, 1.0, X, ldx, 0.0, Xc, ld))) return st;
-        GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
+        GB_LAUNCH(ctx, k_dot_partial<double>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part, a->dinv);
         GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
             GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
         if ((st = bcg_rounds<double>(ctx, A, R, Xc, P, W, ld, a, &s))) return st;
@@ -650,7 +662,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     if ((st = gb_convert_d2f(ctx, n, k, RHS, ldr, R, ld))) return st;
     if (cudaMemsetAsync(D, 0, (size_t)n * ld * sizeof(float), ctx->stream) != cudaSuccess)
         return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
-    GB_LAUNCH(ctx, k_dot_partial<float>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part);
+    GB_LAUNCH(ctx, k_dot_partial<float>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part, a->dinv32);
     GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
     GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
     if ((st = k <= 128 ? bcg_rounds32(ctx, A, R, D, P, W, ld, a, &s) : bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s)))
@@ -670,5 +682,35 @@ extern "C" int gb_axpy32(gcge_gpu_ctx *ctx, int n, int k, float a, const float *
 {
     if (n <= 0 || k <= 0) return GCGE_GPU_OK;
     GB_LAUNCH(ctx, k_axpy32, row_grid(ctx, n), 256, 0, n, k, a, X, Y, ld);
+    return GCGE_GPU_OK;
+}
+
+// ---------------------------------------------------------------- Jacobi preconditioner
+// dinv[r] = 1 / A[r, r] (1 where the row has no nonzero diagonal entry), FP64 and FP32
+__global__ void k_diag_inv(int n, const int *__restrict__ rp, const int *__restrict__ ci,
+                           const double *__restrict__ v, double *__restrict__ dinv, float *__restrict__ dinv32)
+{
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+        double dg = 0.0;
+        for (int e = rp[r]; e < rp[r + 1]; ++e)
+            if (ci[e] == r) dg += v[e];
+        const double di = dg != 0.0 ? 1.0 / dg : 1.0;
+        dinv[r] = di;
+        dinv32[r] = (float)di;
+    }
+}
+
+extern "C" int gb_mat_dinv(gcge_gpu_ctx *ctx, gcge_gpu_mat *A)
+{
+    if (A->dinv) return GCGE_GPU_OK;
+    const size_t n = (size_t)(A->n > 0 ? A->n : 1);
+    if (cudaMalloc(&A->dinv, sizeof(double) * n) != cudaSuccess ||
+        cudaMalloc(&A->dinv32, sizeof(float) * n) != cudaSuccess) {
+        cudaFree(A->dinv);
+        A->dinv = nullptr;
+        A->dinv32 = nullptr;
+        return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
+    }
+    GB_LAUNCH(ctx, k_diag_inv, row_grid(ctx, A->n / 8 + 1), 256, 0, A->n, A->rp, A->ci, A->v, A->dinv, A->dinv32);
     return GCGE_GPU_OK;
 }

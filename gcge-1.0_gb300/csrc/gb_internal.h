@@ -64,6 +64,8 @@ struct gcge_gpu_mat {
     double *v;                 /* device FP64 values */
     float *v32;                /* device FP32 values (mixed precision) or NULL */
     double max_row_nnz;
+    double *dinv;              /* 1 / diag(A) for the Jacobi preconditioner (lazy) or NULL */
+    float *dinv32;             /* the same in FP32 */
 };
 
 struct gcge_gpu_mv {
@@ -140,7 +142,12 @@ typedef struct {
     int n, k, max_it, precision;
     double rate;
     int rhs_is_residual;       /* RHS already holds RHS - A X: skip the initial product */
+    const double *dinv;        /* Jacobi preconditioner 1/diag(A) (FP64 rounds) or NULL: plain CG */
+    const float *dinv32;       /* the same for the FP32 rounds */
 } gb_bcg_args;
+/* 1 / diag(A) in FP64 and FP32, computed once per matrix values (a zero or missing
+ * diagonal entry gives 1) */
+int gb_mat_dinv(gcge_gpu_ctx *ctx, gcge_gpu_mat *A);
 int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, long ldr, double *X, long ldx,
            const gb_bcg_args *args, void *work, size_t work_bytes);
 size_t gb_bcg_work_bytes(int n, int k, int precision);

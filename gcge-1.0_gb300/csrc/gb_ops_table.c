@@ -303,6 +303,78 @@ static void op_DenseMatEigenSolver(char *jobz, char *range, char *uplo, int *nro
     rec(st);
 }
 
+/* ---------------------------------------------------------- LinearSolver hook */
+/* The reference calls ops->LinearSolver(A, b, x, ops) once per W column in place of
+ * its block CG (src/gcge_xpw.c:177-191); its parameters cannot travel through that
+ * signature, so they are set here. Kind 1: Jacobi-preconditioned CG on the device
+ * (the block CG of this library with k = 1 and z = diag(A)^-1 r) from the given x,
+ * to ||r||_z <= rate ||r0||_z or max_it iterations; b is left unchanged. */
+static int g_ls_max_it = 20;
+static double g_ls_rate = 1e-2;
+static gcge_gpu_mv *g_ls_rhs = NULL;     /* copy of b (the block CG overwrites its right-hand side) */
+static void *g_ls_work = NULL;
+static size_t g_ls_work_bytes = 0;
+
+static void op_LinearSolverJacobi(void *mat, void *b, void *x, GCGE_GPU_OPS_LAYOUT *ops)
+{
+    (void)ops;
+    gcge_gpu_mat *A = (gcge_gpu_mat *)mat;
+    gvec *vb = H(b), *vx = H(x);
+    const int n = A->n;
+    int st = 0;
+    if (!g_ctx || vb->mv->n != n || vx->mv->n != n) {
+        rec(GCGE_GPU_ERR_ARG);
+        return;
+    }
+    if (g_ls_rhs && g_ls_rhs->n != n) {
+        GCGE_GPU_MultiVecDestroy(g_ls_rhs);
+        g_ls_rhs = NULL;
+    }
+    if (!g_ls_rhs && (st = GCGE_GPU_MultiVecCreate(g_ctx, n, 1, &g_ls_rhs))) {
+        rec(st);
+        return;
+    }
+    const size_t need = gb_bcg_work_bytes(n, 1, 0);
+    if (need > g_ls_work_bytes) {
+        cudaFree(g_ls_work);
+        g_ls_work = NULL;
+        g_ls_work_bytes = 0;
+        if (cudaMalloc(&g_ls_work, need) != cudaSuccess) {
+            rec(GCGE_GPU_ERR_NOMEM);
+            return;
+        }
+        g_ls_work_bytes = need;
+    }
+    if ((st = gb_mat_dinv(g_ctx, A))) {
+        rec(st);
+        return;
+    }
+    if ((st = gb_axpby(g_ctx, n, 1, 1.0, colptr(vb), vb->mv->ld, 0.0, g_ls_rhs->d, g_ls_rhs->ld))) {
+        rec(st);
+        return;
+    }
+    gb_bcg_args a;
+    memset(&a, 0, sizeof(a));
+    a.n = n;
+    a.k = 1;
+    a.max_it = g_ls_max_it;
+    a.precision = 0;
+    a.rate = g_ls_rate;
+    a.dinv = A->dinv;
+    a.dinv32 = A->dinv32;
+    rec(gb_bcg(g_ctx, A, g_ls_rhs->d, g_ls_rhs->ld, colptr(vx), vx->mv->ld, &a, g_ls_work, g_ls_work_bytes));
+}
+
+int GCGE_GPU_OpsSetLinearSolver(void *gcge_ops, int kind, int max_it, double rate)
+{
+    if (!gcge_ops || kind < 0 || kind > 1 || max_it < 1 || !(rate > 0)) return GCGE_GPU_ERR_ARG;
+    GCGE_GPU_OPS_LAYOUT *ops = (GCGE_GPU_OPS_LAYOUT *)gcge_ops;
+    g_ls_max_it = max_it;
+    g_ls_rate = rate;
+    ops->LinearSolver = kind == 1 ? op_LinearSolverJacobi : NULL;
+    return GCGE_GPU_OK;
+}
+
 int GCGE_GPU_SetOps(gcge_gpu_ctx *ctx, void *table)
 {
     if (!ctx || !table) return GCGE_GPU_ERR_ARG;

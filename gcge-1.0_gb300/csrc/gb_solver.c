@@ -277,6 +277,14 @@ static int compute_w(gcg_t *g)
     a.precision = g->p.precision;
     a.rate = g->p.cg_rate;
     a.rhs_is_residual = 0;
+    a.dinv = NULL;
+    a.dinv32 = NULL;
+    if (g->p.precond == 1) {
+        /* Jacobi: the diagonal inverse is cached on the matrix (recomputed after new values) */
+        TRY(gb_mat_dinv(ctx, (gcge_gpu_mat *)g->A));
+        a.dinv = g->A->dinv;
+        a.dinv32 = g->A->dinv32;
+    }
     if (g->conv_products) {
         /* the convergence check left A x (S2) and B x (S3) of these columns: the
          * initial residual l B w - A w, w = s x, is s (l B x - A x) without a product */

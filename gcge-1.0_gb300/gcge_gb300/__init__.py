@@ -33,7 +33,7 @@ class Params(C.Structure):
                 ("max_reorth_time", C.c_int), ("dirichlet_boundary", C.c_int), ("given_init_evec", C.c_int),
                 ("ev_tol", C.c_double), ("cg_rate", C.c_double), ("orth_zero_tol", C.c_double),
                 ("conv_type", C.c_char * 4), ("precision", C.c_int), ("seed", C.c_ulonglong),
-                ("print_level", C.c_int)]
+                ("print_level", C.c_int), ("precond", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -94,6 +94,7 @@ def load():
         "GCGE_GPU_SetOps": (_I, [_P, _P]),
         "GCGE_GPU_OpsSeed": (None, [C.c_ulonglong]),
         "GCGE_GPU_OpsMultiVecBlock": (_I, [_P, C.POINTER(_P), C.POINTER(_I)]),
+        "GCGE_GPU_OpsSetLinearSolver": (_I, [_P, _I, _I, _D]),
         "GCGE_GPU_ProfileEnable": (_I, [_P, _I]),
         "GCGE_GPU_ProfileRead": (_I, [_P, _I, _P, _P, _P, _P, _I]),
         "GCGE_GPU_SetTensorEmulation": (_I, [_P, _I]),

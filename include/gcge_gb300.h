@@ -151,6 +151,10 @@ typedef struct {
     int    precision;         /* 0 plain FP64; 1 mixed (FP32 inner block CG)          */
     unsigned long long seed;  /* counter-hash seed of the initial vectors             */
     int    print_level;       /* 0 silent; 1 one line per iteration (reference format)*/
+    int    precond;           /* inner block CG: 0 plain (GCGE_BCG, the default);
+                                 1 Jacobi-preconditioned (z = diag(A)^-1 r, rho = r.z),
+                                 the role of a user linear solver installed in
+                                 ops->LinearSolver (src/gcge_xpw.c:177-191)          */
 } gcge_gpu_params;
 
 typedef struct {

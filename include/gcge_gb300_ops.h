@@ -28,7 +28,8 @@
  * dsyevx-signature eigensolve, run on the device). The small dense BLAS members
  * (DenseMatDotDenseMat, DenseSymMatDotDenseMat, Array*) are left as they are,
  * so GCGE_OPS_Setup (src/gcge_ops.c:573-604) installs its host defaults.
- * LinearSolver and Orthonormalization are left as they are.
+ * Orthonormalization is left as it is; LinearSolver is left unset unless
+ * GCGE_GPU_OpsSetLinearSolver installs a device solver there.
  *
  * The members return void, as in the reference; failures are recorded on the
  * context and read with GCGE_GPU_GetLastError after GCGE_SOLVER_Solve.
@@ -106,6 +107,16 @@ void GCGE_GPU_OpsSeed(unsigned long long seed);
 /* Device multivector behind a table multivector handle (void **), with the
  * column its first handle refers to. */
 int GCGE_GPU_OpsMultiVecBlock(void **multi_vec, gcge_gpu_mv **block, int *first_col);
+
+/* Install a device linear solver in the table's LinearSolver member, which the
+ * reference calls once per W column in place of its block CG
+ * (src/gcge_xpw.c:177-191): kind 0 removes it (the reference's GCGE_BCG runs),
+ * kind 1 installs Jacobi-preconditioned CG (z = diag(A)^-1 r) run from the given
+ * x to ||r||_z <= rate ||r0||_z or max_it iterations (b is left unchanged). The
+ * reference's hook signature (A, b, x, ops) carries no parameters, so max_it and
+ * rate are held by the library for every table. No counterpart in the reference
+ * beyond the hook itself (its users install HYPRE solvers there). */
+int GCGE_GPU_OpsSetLinearSolver(void *gcge_ops, int kind, int max_it, double rate);
 
 #ifdef __cplusplus
 }

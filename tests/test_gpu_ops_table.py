@@ -177,3 +177,31 @@ def test_table_dense_eigensolver_matches_lapack(env, m):
     np.testing.assert_allclose(ev[:k], w[:k], rtol=1e-12, atol=1e-12 * np.abs(w).max())
     for j in range(k):
         assert abs(abs(Z[j, :m] @ U[:, j]) - 1.0) < 1e-10
+
+
+def test_table_linear_solver_hook(env):
+    """GCGE_GPU_OpsSetLinearSolver installs a device Jacobi-preconditioned CG in the
+    table's LinearSolver member (the hook GCGE calls per W column in place of its
+    block CG, src/gcge_xpw.c:177-191); kind 0 removes it."""
+    ctx, tab = env
+    import scipy.sparse.linalg as spla
+    A, _ = P.varcoef2d(nc=40, seed=3, sigma=1.0)
+    n = A.n
+    dA = ctx.matrix(A)
+    rng = np.random.default_rng(14)
+    b = rng.standard_normal(n)
+    assert ctx.lib.GCGE_GPU_OpsSetLinearSolver(C.byref(tab), 1, 5000, 1e-12) == 0
+    assert tab.LinearSolver
+    solve = C.CFUNCTYPE(None, V_, V_, V_, V_)(tab.LinearSolver)
+    h = mv_create(ctx, tab, dA, 2)
+    mv_upload(ctx, h, np.stack([b, np.zeros(n)], axis=1))
+    solve(dA.h, h[0], h[1], C.cast(C.byref(tab), V_))
+    assert ctx.last_error() == 0
+    out = mv_download(ctx, h, 2, n)
+    assert np.array_equal(out[:, 0], b)                      # the right-hand side is left as it was
+    x_ref = spla.spsolve(A.to_scipy().tocsc(), b)
+    assert np.linalg.norm(out[:, 1] - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+    tab.MultiVecDestroy(C.byref(h), 2, None)
+    assert ctx.lib.GCGE_GPU_OpsSetLinearSolver(C.byref(tab), 0, 20, 1e-2) == 0
+    assert not tab.LinearSolver
+    assert ctx.lib.GCGE_GPU_OpsSetLinearSolver(C.byref(tab), 2, 20, 1e-2) == 1

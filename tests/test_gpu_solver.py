@@ -207,6 +207,27 @@ def test_varcoef3d_mixed(ctx, oracle):
     assert np.all(residuals(A, B, ev, X, "BR") <= 1.05e-8)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_jacobi_preconditioned_inner_solve(ctx, oracle, precision):
+    """precond = 1 (the role of a linear solver installed in ops->LinearSolver):
+    Jacobi-preconditioned block CG gives the same eigenpairs as the oracle in no
+    more outer iterations than plain block CG on a variable-coefficient problem."""
+    A, B = P.varcoef3d(nc=16, seed=21)
+    dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
+    its = {}
+    for pc in (0, 1):
+        ev, X, st = ctx.solve(dA, dB, ctx.params(nev=20, block_size=24, seed=8, conv_type="BR", ev_max_it=500,
+                                                 precision=precision, precond=pc))
+        assert st.num_unlock == 0
+        assert np.all(residuals(A, B, ev, X, "BR") <= 1.05e-8)
+        its[pc] = st.num_iter
+        if pc == 1:
+            oe, oX, ost = oracle.solve(A, B, oracle.params(nev=24, conv_type="BR", ev_tol=1e-11, ev_max_it=800,
+                                                           init_rng=1, seed=4))
+            assert np.max(np.abs(ev - oe[:20]) / np.abs(oe[:20])) < 1e-9
+    assert its[1] <= its[0], its
+
+
 def test_irregular_graph_mixed(ctx, oracle):
     """Power-law graph Laplacian (irregular rows up to 300 nonzeros), B = diag U[1,2]."""
     A, B = P.powerlaw_graph(4000, seed=11, dmax=300)
