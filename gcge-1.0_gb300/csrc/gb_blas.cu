@@ -293,9 +293,16 @@ extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X
     ctx->spmm_launches++;
     GB_PROF(ctx, GB_K_SPMM64, 12.0 * A->nnz + 4.0 * (A->n + 1) + (beta != 0.0 ? 24.0 : 16.0) * A->n * k,
             2.0 * A->nnz * k);
-    // one column: a warp per row for long rows; short rows (stencils) go to the
-    // lane-group kernel, 4 lanes per row
-    if (k == 1 && (double)A->nnz > 16.0 * A->n) {
+    // one column: matrices whose longest row is short (stencils, meshes) take a
+    // thread per row -- a warp-wide reduction per row would cost five FP64 adds on
+    // every lane, and the FP64 pipe is the narrow one; long rows keep a warp per row
+    if (k == 1) {
+        if (A->max_row_nnz <= 64.0) {
+            const int grid = ceil_div_l((long)A->n, 256);
+            GB_LAUNCH(ctx, (k_spmm64_lv<1, 1>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx, Y, ldy, 1, alpha,
+                      alpha_col, beta, ncols_dev);
+            return GCGE_GPU_OK;
+        }
         int grid = ceil_div_l((long)A->n * 32, 256);
         GB_LAUNCH(ctx, (k_spmv<double, double, double>), grid, 256, 0, A->n, A->rp, A->ci, A->v, X, ldx,
                   Y, ldy, alpha, alpha_col, beta, ncols_dev);
@@ -543,9 +550,12 @@ template <int MODE>
 __global__ void __launch_bounds__(256)
 k_coldot_partial(int n, int k, const double *__restrict__ X, long ldx, const double *__restrict__ Y, long ldy,
                  const double *__restrict__ Z, long ldz, const double *__restrict__ eval,
-                 const int *__restrict__ idx, double *__restrict__ part)
+                 const int *__restrict__ idx, double *__restrict__ part, int bnorm = 0)
 {
-    // MODE 0: sum X*Y. MODE 1: residual triple (sum (Y - l Z)^2, sum X^2, sum Z^2), Z may be NULL (= X).
+    // MODE 0: sum X*Y. MODE 1: residual triple (sum (Y - l Z)^2, sum X^2, sum Z^2), Z may be NULL (= X);
+    // bnorm != 0 ("BR": only the residual and the B-norm are used) skips X (when Z is given) and sum X^2
+    // (reported as sum Z^2): three FP64 operations per entry instead of four, the FP64 pipe being the
+    // limit of this pass on GB300
     __shared__ double sh[3][8][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int c = blockIdx.y * 32 + tx;
@@ -558,13 +568,17 @@ k_coldot_partial(int n, int k, const double *__restrict__ X, long ldx, const dou
         for (long r = r0 + ty; r < r1; r += 8) {
             if (MODE == 0) {
                 s0 = fma(X[r * ldx + c], Y[r * ldy + c], s0);
+            } else if (bnorm) {
+                const double bx = Z ? Z[r * ldz + c] : X[r * ldx + c];
+                const double res = Y[r * ldy + c] - l * bx;
+                s0 = fma(res, res, s0);
+                s2 = fma(bx, bx, s2);
             } else {
                 const double x = X[r * ldx + c];
                 const double bx = Z ? Z[r * ldz + c] : x;
                 const double res = Y[r * ldy + c] - l * bx;
                 s0 = fma(res, res, s0);
                 s1 = fma(x, x, s1);
-                s2 = fma(bx, bx, s2);
             }
         }
     }
@@ -575,6 +589,10 @@ k_coldot_partial(int n, int k, const double *__restrict__ X, long ldx, const dou
     if (ty == 0 && c < k) {
         double t0 = 0, t1 = 0, t2 = 0;
         for (int q = 0; q < 8; ++q) { t0 += sh[0][q][tx]; t1 += sh[1][q][tx]; t2 += sh[2][q][tx]; }
+        if (MODE == 1) {
+            if (bnorm) t1 = t2;                       // only the B-norm was formed
+            else t2 = t1;                             // only the 2-norm was formed
+        }
         const int w = MODE == 0 ? 1 : 3;
         double *p = part + ((long)blockIdx.x * k + c) * w;
         p[0] = t0;
@@ -608,16 +626,16 @@ extern "C" int gb_col_dots(gcge_gpu_ctx *ctx, int n, int k, const double *X, lon
 
 extern "C" int gb_residual_norms(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, const double *AX,
                                  long ldax, const double *BX, long ldbx, const double *eval_dev,
-                                 const int *idx_dev, double *out_dev)
+                                 const int *idx_dev, double *out_dev, int bnorm)
 {
     if (k <= 0) return GCGE_GPU_OK;
     const int nblk = ceil_div_l(n > 0 ? n : 1, RED_ROWS);
     int st = gb_scratch(ctx, (size_t)nblk * k * 3);
     if (st) return st;
     dim3 grid(nblk, (k + 31) / 32);
-    GB_PROF(ctx, GB_K_REDUCE, (BX ? 24.0 : 16.0) * n * k, 8.0 * n * k);
+    GB_PROF(ctx, GB_K_REDUCE, (BX && !bnorm ? 24.0 : 16.0) * n * k, 6.0 * n * k);
     GB_LAUNCH(ctx, k_coldot_partial<1>, grid, 256, 0, n, k, X, ldx, AX, ldax, BX, ldbx, eval_dev, idx_dev,
-              ctx->scratch);
+              ctx->scratch, bnorm);
     GB_LAUNCH(ctx, k_sum_partials, (3 * k + 127) / 128, 128, 0, nblk, 3 * k, ctx->scratch, out_dev);
     return GCGE_GPU_OK;
 }

@@ -37,54 +37,44 @@
     } while (0)
 
 // ---------------------------------------------------------------- small GEMM
+// C = alpha op(A) op(B) + beta C for the projected matrices (m, n, k of a few hundred
+// at most). FP64 on GB300 is narrow (~2 FMA per clock per SM) and a dependent FP64
+// chain costs ~40 ns per step, so the work is spread thin: an 8 x 8 tile of C per
+// block, 256 threads = 64 outputs x 4 slices of the inner dimension, each slice
+// accumulated in two interleaved chains (k / 8 dependent steps), the slices summed
+// in a fixed order in shared memory.
+#define SG_T 8
 __global__ void __launch_bounds__(256)
 k_small_gemm(char ta, char tb, int m, int n, int k, double alpha, const double *__restrict__ A, int lda,
              const double *__restrict__ B, int ldb, double beta, double *__restrict__ C, int ldc)
 {
-    __shared__ double As[32][33];
-    __shared__ double Bs[32][33];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-    double acc[4] = {0, 0, 0, 0};
-    for (int l0 = 0; l0 < k; l0 += 32) {
-        for (int e = threadIdx.x; e < 1024; e += 256) {
-            const int a = e & 31, b = e >> 5;  // a fastest
-            // As[i][l]: op(A)(i0+i, l0+l)
-            {
-                const int i = a, l = b;
-                const int gi = i0 + i, gl = l0 + l;
-                double v = 0;
-                if (gi < m && gl < k) v = (ta == 'N') ? A[gi + (long)gl * lda] : A[gl + (long)gi * lda];
-                As[i][l] = v;
-            }
-            // Bs[l][j]: op(B)(l0+l, j0+j)
-            {
-                const int l = a, j = b;
-                const int gl = l0 + l, gj = j0 + j;
-                double v = 0;
-                if (gl < k && gj < n) v = (tb == 'N') ? B[gl + (long)gj * ldb] : B[gj + (long)gl * ldb];
-                Bs[l][j] = v;
-            }
+    __shared__ double part[4][SG_T * SG_T];
+    const int t = threadIdx.x, o = t & 63, sl = t >> 6;
+    const int i = blockIdx.x * SG_T + (o & 7), j = blockIdx.y * SG_T + (o >> 3);
+    double a0 = 0, a1 = 0;
+    if (i < m && j < n) {
+        const bool an = ta == 'N', bn = tb == 'N';
+        int l = sl;
+        for (; l + 4 < k; l += 8) {
+            const double x0 = an ? A[i + (long)l * lda] : A[l + (long)i * lda];
+            const double y0 = bn ? B[l + (long)j * ldb] : B[j + (long)l * ldb];
+            const double x1 = an ? A[i + (long)(l + 4) * lda] : A[(l + 4) + (long)i * lda];
+            const double y1 = bn ? B[(l + 4) + (long)j * ldb] : B[j + (long)(l + 4) * ldb];
+            a0 = fma(x0, y0, a0);
+            a1 = fma(x1, y1, a1);
         }
-        __syncthreads();
-#pragma unroll 4
-        for (int l = 0; l < 32; ++l) {
-            const double a = As[tx][l];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[q] = fma(a, Bs[l][ty + 8 * q], acc[q]);
+        if (l < k) {
+            const double x0 = an ? A[i + (long)l * lda] : A[l + (long)i * lda];
+            const double y0 = bn ? B[l + (long)j * ldb] : B[j + (long)l * ldb];
+            a0 = fma(x0, y0, a0);
         }
-        __syncthreads();
     }
-    const int i = i0 + tx;
-    if (i < m) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int j = j0 + ty + 8 * q;
-            if (j < n) {
-                double *c = C + i + (long)j * ldc;
-                *c = beta == 0.0 ? alpha * acc[q] : alpha * acc[q] + beta * *c;
-            }
-        }
+    part[sl][o] = a0 + a1;
+    __syncthreads();
+    if (sl == 0 && i < m && j < n) {
+        const double acc = (part[0][o] + part[1][o]) + (part[2][o] + part[3][o]);
+        double *c = C + i + (long)j * ldc;
+        *c = beta == 0.0 ? alpha * acc : alpha * acc + beta * *c;
     }
 }
 
@@ -92,7 +82,7 @@ extern "C" int gb_small_gemm(gcge_gpu_ctx *ctx, char ta, char tb, int m, int n, 
                              const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc)
 {
     if (m <= 0 || n <= 0) return GCGE_GPU_OK;
-    dim3 grid((m + 31) / 32, (n + 31) / 32);
+    dim3 grid((m + SG_T - 1) / SG_T, (n + SG_T - 1) / SG_T);
     GB_PROF(ctx, GB_K_DENSE, 8.0 * ((double)m * k + (double)k * n + (double)m * n), 2.0 * m * n * (double)k);
     GB_LAUNCH(ctx, k_small_gemm, grid, 256, 0, ta, tb, m, n, k > 0 ? k : 0, alpha, A, lda, B, ldb, beta, C, ldc);
     return GCGE_GPU_OK;

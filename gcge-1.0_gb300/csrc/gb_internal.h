@@ -117,10 +117,12 @@ int gb_col_dots(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, cons
                 double *out_dev);
 /* residual norms for the convergence test: for c < k with l = eval[idx[c]]
  * out[3c+0] = ||AX_c - l BX_c||^2, out[3c+1] = ||X_c||^2, out[3c+2] = ||BX_c||^2
- * (BX == NULL means B = I) */
+ * (BX == NULL means B = I); bnorm != 0 forms only the first and the last (the
+ * middle slot then repeats the last), otherwise only the first two (the last
+ * repeats the middle) */
 int gb_residual_norms(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx, const double *AX,
                       long ldax, const double *BX, long ldbx, const double *eval_dev, const int *idx_dev,
-                      double *out_dev);
+                      double *out_dev, int bnorm);
 /* a[i + j*lda] = sum_r V[r,i] W[r,j], i < k1, j < k2 (sym: i <= j computed, mirrored) */
 int gb_gram(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *V, long ldv, const double *W, long ldw,
             double *a_dev, int lda, int sym);

@@ -197,7 +197,7 @@ static int check_conv(gcg_t *g)
         TRY(gb_spmm(ctx, g->A, g->S1, g->lds, g->S2, g->lds, nu, 1.0, NULL, 0.0, NULL));
         if (g->B) TRY(gb_spmm(ctx, g->B, g->S1, g->lds, g->S3, g->lds, nu, 1.0, NULL, 0.0, NULL));
         TRY(gb_residual_norms(ctx, n, nu, g->S1, g->lds, g->S2, g->lds, g->B ? g->S3 : NULL, g->lds, g->eval_d,
-                              g->unlock_d, g->res_d));
+                              g->unlock_d, g->res_d, strcmp(g->p.conv_type, "BR") == 0));
         CTRY(cudaMemcpyAsync(g->res_h, g->res_d, sizeof(double) * 3 * nu, cudaMemcpyDeviceToHost, ctx->stream));
     }
     CTRY(cudaMemcpyAsync(g->eval_h, g->eval_d, sizeof(double) * g->V_size, cudaMemcpyDeviceToHost, ctx->stream));
