@@ -247,7 +247,7 @@ def run_gb300(args, dist):
         return ev, Xh, st
 
     for _ in range(args.warmup):
-        solve(1)
+        solve(args.precision)
     # ---- timed region: K mixed-precision solves, profiling on (events on the library's stream)
     sampler = ClockSampler(dist.local)
     ctx.profile(True)
@@ -258,7 +258,7 @@ def run_gb300(args, dist):
     t0 = time.time()
     times, iters, launches = [], [], 0
     for _ in range(args.steps):
-        ev, Xh, st = solve(1)
+        ev, Xh, st = solve(args.precision)
         times.append(st.solve_ms * 1e-3)
         iters.append(st.num_iter)
         launches += st.kernel_launches
@@ -287,7 +287,7 @@ def run_gb300(args, dist):
     h2d = A.rowptr.nbytes + A.col.nbytes + A.val.nbytes + B.rowptr.nbytes + B.col.nbytes + B.val.nbytes
     d2h = A.n * nev * 8 + nev * 8
     for i in range((1 + args.e2e_steps) if args.e2e_steps else 0):
-        p = params(1)
+        p = params(args.precision)
         ctx.sync()
         t = time.time()
         ctx.solve_host(A, B, p)
@@ -297,7 +297,7 @@ def run_gb300(args, dist):
     # ---- supplementary: the same mixed solve with the Jacobi-preconditioned inner block CG
     # (the role of a solver installed in ops->LinearSolver); not the headline, which keeps
     # the reference's plain block CG
-    pj = params(1)
+    pj = params(args.precision)
     pj.precond = 1
     evj, Xj, stj = ctx.solve(dA, dB, pj, evec=X)
     resj, errj = check_solution(A, B, evj, Xj, exact)
@@ -318,12 +318,13 @@ def run_gb300(args, dist):
         out = {
             "metric": METRIC, "value": mixed_s, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": mixed_s * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp64 + fp32 inner block CG",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64 + fp32 inner block CG" + (" + fp32-pair outer SpMM" if args.precision == 2 else ""),
             "data": "synthetic (exactly assembled Q1 FEM pencil, closed-form spectrum)",
             "config": {"workload": "Q1 FEM cube %d^3 elements, n=%d, nnz(A)=%d, nnz(B)=%d, nev=%d, block=%d, "
                                    "residual ||Ax-lBx||/(|l||Bx||)<=1e-8" % (WORKLOADS[args.workload][0], A.n,
                                                                               A.nnz, B.nnz, nev, block),
-                       "form": "mixed", "parallelism": "replicas" if dist.world > 1 else "single GPU",
+                       "form": "mixed (precision %d)" % args.precision, "parallelism": "replicas" if dist.world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (A+B %.0f MB > 129 MB)" % (h2d / 1e6),
                        "problem_generation_s": gen_s},
             "fp64": {"value": fp64_s, "unit": "s", "iterations": fp64_iters, "max_residual": res64,
@@ -399,8 +400,9 @@ def run_kernel(args):
         Msp = A if args.kernel == "spmm_a" else B
         M, k, n = ctx.matrix(Msp), args.k, A.n
         X, Y = ctx.multivec(n, k, rng.standard_normal((n, k))), ctx.multivec(n, k)
+        ctx.pair_spmm(args.pair)
         op = lambda: G.mat_dot_multivec(M, X, Y, (0, 0), (k, k))
-        flops, desc = 2.0 * Msp.nnz * k, "n=%d nnz=%d k=%d" % (n, Msp.nnz, k)
+        flops, desc = 2.0 * Msp.nnz * k, "n=%d nnz=%d k=%d %s" % (n, Msp.nnz, k, "fp32-pair" if args.pair else "fp64")
     elif args.kernel == "bcg32":
         A, _ = P.fem_q1_cube(args.ne)
         M, k, n = ctx.matrix(A, keep_fp32=True), args.k, A.n
@@ -530,6 +532,9 @@ def main():
     ap.add_argument("--k", type=int, default=64, help="columns for --kernel spmm_a/spmm_b/bcg32")
     ap.add_argument("--nc", type=int, default=None, help="cells per edge for --kernel adjoint (512) / c3 (160)")
     ap.add_argument("--precond", type=int, default=0, help="inner block CG for --kernel c3/c5: 0 plain, 1 Jacobi")
+    ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
+                    help="mixed form of the headline solve: 1 FP32 inner block CG; 2 also FP32-pair outer products")
+    ap.add_argument("--pair", type=int, default=0, help="--kernel spmm_a/spmm_b: 1 FP32-pair product")
     args = ap.parse_args()
     if args.nc is None:
         args.nc = 160 if args.kernel == "c3" else 512

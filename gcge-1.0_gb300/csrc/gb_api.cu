@@ -113,6 +113,13 @@ extern "C" int GCGE_GPU_SetTensorEmulation(gcge_gpu_ctx *ctx, int on)
     return GCGE_GPU_OK;
 }
 
+extern "C" int GCGE_GPU_SetPairSpMM(gcge_gpu_ctx *ctx, int on)
+{
+    if (!ctx) return GCGE_GPU_ERR_ARG;
+    ctx->spmm_pair = on ? 1 : 0;
+    return GCGE_GPU_OK;
+}
+
 // ---------------------------------------------------------------- context
 extern "C" int GCGE_GPU_Init(int device, gcge_gpu_ctx **out)
 {
@@ -137,7 +144,9 @@ extern "C" int GCGE_GPU_Init(int device, gcge_gpu_ctx **out)
     if (!st) st = gb_pinned(c, 1 << 16);
     if (!st) st = gb_ozbuf(c, 1 << 20);
     if (!st && (cudaMalloc(&c->dev_err, sizeof(int)) != cudaSuccess ||
-                cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream) != cudaSuccess))
+                cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream) != cudaSuccess ||
+                cudaMalloc(&c->dev_pairflag, sizeof(int)) != cudaSuccess ||
+                cudaMemsetAsync(c->dev_pairflag, 0, sizeof(int), c->stream) != cudaSuccess))
         st = GCGE_GPU_ERR_NOMEM;
     if (st) {
         GCGE_GPU_Finalize(c);
@@ -165,6 +174,8 @@ extern "C" int GCGE_GPU_Finalize(gcge_gpu_ctx *ctx)
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->ozbuf) cudaFree(ctx->ozbuf);
     if (ctx->dev_err) cudaFree(ctx->dev_err);
+    if (ctx->dev_pairflag) cudaFree(ctx->dev_pairflag);
+    if (ctx->pairbuf) cudaFree(ctx->pairbuf);
     cudaStreamDestroy(ctx->stream);
     free(ctx);
     return GCGE_GPU_OK;
@@ -343,12 +354,16 @@ extern "C" int GCGE_GPU_MatSetValues(gcge_gpu_mat *A, const double *val)
     gcge_gpu_ctx *ctx = A->ctx;
     if (!A->nnz) return GCGE_GPU_OK;
     CUDA_TRY(ctx, cudaMemcpyAsync(A->v, val, sizeof(double) * A->nnz, cudaMemcpyHostToDevice, ctx->stream));
-    if (A->dinv) {                         // the Jacobi diagonal follows the values
+    if (A->dinv || A->vpair) {             // the Jacobi diagonal and the pairs follow the values
         cudaStreamSynchronize(ctx->stream);
-        cudaFree(A->dinv);
-        cudaFree(A->dinv32);
+        if (A->dinv) cudaFree(A->dinv);
+        if (A->dinv32) cudaFree(A->dinv32);
+        if (A->vpair) cudaFree(A->vpair);
+        if (A->pair_meta) cudaFree(A->pair_meta);
         A->dinv = nullptr;
         A->dinv32 = nullptr;
+        A->vpair = nullptr;
+        A->pair_meta = nullptr;
     }
     if (A->v32) {
         k_d2f_vals<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(A->nnz, A->v, A->v32);
@@ -369,6 +384,8 @@ extern "C" int GCGE_GPU_MatDestroy(gcge_gpu_mat *A)
     if (A->v32) cudaFree(A->v32);
     if (A->dinv) cudaFree(A->dinv);
     if (A->dinv32) cudaFree(A->dinv32);
+    if (A->vpair) cudaFree(A->vpair);
+    if (A->pair_meta) cudaFree(A->pair_meta);
     free(A);
     return GCGE_GPU_OK;
 }

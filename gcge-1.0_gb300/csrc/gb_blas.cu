@@ -197,21 +197,13 @@ k_spmv(int n, const int *__restrict__ rp, const int *__restrict__ ci, const VT *
 // lane runs the same instruction stream: a lane whose columns run past k reads
 // the window [k - VW, k) instead (VW <= k, so it stays inside the range) and
 // stores only the columns it owns, so that no lane diverges in the inner loop.
+// one row group of the FP64 SpMM below: the L lanes of group `sub` own row `row`
 template <int L, int VW>
-__global__ void __launch_bounds__(256)
-k_spmm64_lv(int n, const int *__restrict__ rp, const int *__restrict__ ci, const double *__restrict__ val,
-            const double *__restrict__ X, long ldx, double *__restrict__ Y, long ldy, int k, double alpha,
-            const double *__restrict__ alpha_col, double beta, const int *__restrict__ ncols_dev)
+__device__ __forceinline__ void
+spmm64_row(long row, int sl, unsigned gmask, int kact, int k, const int *__restrict__ rp,
+           const int *__restrict__ ci, const double *__restrict__ val, const double *__restrict__ X, long ldx,
+           double *__restrict__ Y, long ldy, double alpha, const double *__restrict__ alpha_col, double beta)
 {
-    constexpr int RPW = 32 / L;
-    const int lane = threadIdx.x & 31;
-    const int sub = lane / L, sl = lane % L;
-    const unsigned gmask = (L == 32) ? FULL : (((1u << L) - 1u) << (sub * L));
-    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long row = warp * RPW + sub;
-    int kact = k;
-    if (ncols_dev) kact = min(k, *ncols_dev);
-    if (row >= n || kact <= 0) return;                    // uniform within the row group
     const int beg = rp[row], end = rp[row + 1];
     for (int c0 = 0; c0 < kact; c0 += L * VW) {
         const int c = c0 + sl * VW;                       // first column this lane owns
@@ -241,6 +233,187 @@ k_spmm64_lv(int n, const int *__restrict__ rp, const int *__restrict__ ci, const
             if (col < c || col >= kact) continue;
             const double s = alpha * (alpha_col ? alpha_col[col] : 1.0);
             yr[q] = beta == 0.0 ? s * acc[q] : s * acc[q] + beta * yr[q];
+        }
+    }
+}
+
+template <int L, int VW>
+__global__ void __launch_bounds__(256)
+k_spmm64_lv(int n, const int *__restrict__ rp, const int *__restrict__ ci, const double *__restrict__ val,
+            const double *__restrict__ X, long ldx, double *__restrict__ Y, long ldy, int k, double alpha,
+            const double *__restrict__ alpha_col, double beta, const int *__restrict__ ncols_dev)
+{
+    constexpr int RPW = 32 / L;
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / L, sl = lane % L;
+    const unsigned gmask = (L == 32) ? FULL : (((1u << L) - 1u) << (sub * L));
+    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long row = warp * RPW + sub;
+    int kact = k;
+    if (ncols_dev) kact = min(k, *ncols_dev);
+    if (row >= n || kact <= 0) return;                    // uniform within the row group
+    spmm64_row<L, VW>(row, sl, gmask, kact, k, rp, ci, val, X, ldx, Y, ldy, alpha, alpha_col, beta);
+}
+
+// ---------------------------------------------------------------- FP32-pair SpMM
+// The FP64 product Y = A X computed on the FP32 pipe, which GB300 issues ~64x
+// faster than FP64. Every value is held as an unevaluated sum hi + lo of two
+// floats (a 48-bit significand): A once per matrix, scaled by a power of two 2^-s
+// so that |a| < 1; X split per call. Each term a x is formed with the error-free
+// product of the leading parts (hi*hi exactly as p + e by one FMA, Dekker /
+// Kahan's TwoProduct) plus the two cross terms, and summed into a (hi, lo) pair
+// per output by Knuth's TwoSum (the pair renormalised after every L terms), so
+// the roundings left are the ~2^-48 relative ones of the splits, of the cross
+// terms and of the low-order accumulator -- ~1e-14 of sum |a_ij x_j| against
+// ~1e-16 for FP64. Results are rebuilt as doubles (exponent shifted back
+// by s) with one FP64 add per output. Operations are written with the _rn
+// intrinsics so that the compiler does not contract them into FMAs.
+// Range: x with |x| >= 2^100 (or non-finite) marks the split, and the product
+// then runs the FP64 loop above instead (a device-side switch, uniform per
+// launch); |x| < 2^-126 is flushed to zero, |x| < 2^-74 keeps only its leading
+// part -- absolute errors below 2^-97 |a| on entries that small.
+
+// (hi, lo) of one double by bit manipulation (no FP64 instruction): hi keeps the
+// leading 24 significand bits (truncated), lo the remaining 29 rounded to 24
+__device__ __forceinline__ float2 pair_split(double x, int &bad)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7ff);
+    const unsigned sign = hi & 0x80000000u;
+    if (e >= 1023 + 100) { bad = 1; return make_float2(0.f, 0.f); }
+    if (e < 1023 - 126) return make_float2(0.f, 0.f);
+    const unsigned hb = sign | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    float l = 0.f;
+    const unsigned rem = lo & 0x1fffffffu;
+    if (e >= 949 && rem) l = __fmul_rn(__uint2float_rn(rem), __uint_as_float(sign | ((unsigned)(e - 948) << 23)));
+    return make_float2(__uint_as_float(hb), l);
+}
+
+// f * 2^s exactly as a double (f normal or zero; subnormal f flushes to zero)
+__device__ __forceinline__ double pair_f2d(float f, int s)
+{
+    const unsigned b = __float_as_uint(f);
+    const int e8 = (int)((b >> 23) & 0xff);
+    if (e8 == 0) return 0.0;
+    const unsigned hi = (b & 0x80000000u) | ((unsigned)(e8 + 896 + s) << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)((b & 7u) << 29));
+}
+
+// split an n x k block of X (leading dimension ldx) into pairs, leading dimension k
+__global__ void __launch_bounds__(256)
+k_pair_split(int n, int k, const double *__restrict__ X, long ldx, float2 *__restrict__ Xs, int *flag, int epoch)
+{
+    int bad = 0;
+    const long total = (long)n * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k;
+        const int c = (int)(t - r * k);
+        Xs[t] = pair_split(X[r * ldx + c], bad);
+    }
+    if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) *flag = epoch;
+}
+
+// matrix values: max |a| (as ordered bits of a non-negative double), then the split
+__global__ void k_pair_absmax(int nnz, const double *__restrict__ v, unsigned long long *meta)
+{
+    unsigned long long m = 0;
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (long)gridDim.x * blockDim.x) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(v[e]));
+        m = b > m ? b : m;
+    }
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(FULL, m, o);
+        m = w > m ? w : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(meta, m);
+}
+
+__global__ void k_pair_vals(int nnz, const double *__restrict__ v, float2 *__restrict__ vp, int *meta)
+{
+    const unsigned long long mb = *(const unsigned long long *)meta;
+    // s with max |a| 2^-s in [0.5, 1); s = 0 for an all-zero matrix; non-finite
+    // values or |s| > 700 leave s = 4096, which sends every product to the FP64 loop
+    int s = 0;
+    const int em = (int)((mb >> 52) & 0x7ff);
+    if (em == 0x7ff) s = 4096;
+    else if (mb) s = em - 1022;
+    if (s != 4096 && (s > 700 || s < -700)) s = 4096;
+    if (blockIdx.x == 0 && threadIdx.x == 0) meta[2] = s;
+    if (s == 4096) return;
+    const double sc = ldexp(1.0, -s);
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (long)gridDim.x * blockDim.x) {
+        const double a = v[e] * sc;
+        const float h = __double2float_rn(a);
+        vp[e] = make_float2(h, __double2float_rn(a - (double)h));
+    }
+}
+
+template <int L, int VW>
+__global__ void __launch_bounds__(256)
+k_spmm_pair(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float2 *__restrict__ vp,
+            const int *__restrict__ meta, const float2 *__restrict__ Xs, const double *__restrict__ val,
+            const double *__restrict__ X, long ldx, double *__restrict__ Y, long ldy, int k,
+            const int *__restrict__ flag, int epoch)
+{
+    constexpr int RPW = 32 / L;
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / L, sl = lane % L;
+    const unsigned gmask = (L == 32) ? FULL : (((1u << L) - 1u) << (sub * L));
+    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long row = warp * RPW + sub;
+    if (row >= n) return;                                 // uniform within the row group
+    const int s = meta[2];
+    if (*flag == epoch || s == 4096) {                    // out of the pair range: FP64
+        spmm64_row<L, VW>(row, sl, gmask, k, k, rp, ci, val, X, ldx, Y, ldy, 1.0, nullptr, 0.0);
+        return;
+    }
+    const int beg = rp[row], end = rp[row + 1];
+    for (int c0 = 0; c0 < k; c0 += L * VW) {
+        const int c = c0 + sl * VW;
+        const int cb = min(c, k - VW);
+        float sh[VW], sw[VW];
+#pragma unroll
+        for (int q = 0; q < VW; ++q) { sh[q] = 0.f; sw[q] = 0.f; }
+        for (int base = beg; base < end; base += L) {
+            const int e = base + sl;
+            int j = 0;
+            float2 a = make_float2(0.f, 0.f);
+            if (e < end) { j = __ldg(ci + e); a = __ldg(vp + e); }
+            const int cnt = min(L, end - base);
+#pragma unroll 2
+            for (int t = 0; t < cnt; ++t) {
+                const int jj = __shfl_sync(gmask, j, t, L);
+                const float ah = __shfl_sync(gmask, a.x, t, L);
+                const float al = __shfl_sync(gmask, a.y, t, L);
+                const float2 *xr = Xs + (long)jj * k + cb;
+#pragma unroll
+                for (int q = 0; q < VW; ++q) {
+                    const float2 x = __ldg(xr + q);
+                    const float p = __fmul_rn(ah, x.x);
+                    float er = fmaf(ah, x.x, -p);                 // ah xh - p, exact
+                    er = fmaf(ah, x.y, er);
+                    er = fmaf(al, x.x, er);
+                    const float t1 = __fadd_rn(sh[q], p);           // TwoSum(sh, p)
+                    const float z = __fsub_rn(t1, sh[q]);
+                    const float d = __fadd_rn(__fsub_rn(sh[q], __fsub_rn(t1, z)), __fsub_rn(p, z));
+                    sh[q] = t1;
+                    sw[q] = __fadd_rn(sw[q], __fadd_rn(d, er));
+                }
+            }
+            // renormalise after every L terms (FastTwoSum): |sw| stays near ulp(sh)
+#pragma unroll
+            for (int q = 0; q < VW; ++q) {
+                const float s2 = __fadd_rn(sh[q], sw[q]);
+                sw[q] = __fsub_rn(sw[q], __fsub_rn(s2, sh[q]));
+                sh[q] = s2;
+            }
+        }
+        double *yr = Y + row * ldy + cb;
+#pragma unroll
+        for (int q = 0; q < VW; ++q) {
+            const int col = cb + q;
+            if (col < c || col >= k) continue;
+            yr[q] = pair_f2d(sh[q], s) + pair_f2d(sw[q], s);
         }
     }
 }
@@ -285,11 +458,109 @@ static int spmm64_lv_launch(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const doub
     return gb_fail(ctx, GCGE_GPU_ERR_ARG);
 }
 
+// ---- FP32-pair path: per-matrix pairs (lazy), per-call split of X
+static int pair_mat(gcge_gpu_ctx *ctx, const gcge_gpu_mat *Ac)
+{
+    gcge_gpu_mat *A = (gcge_gpu_mat *)Ac;
+    if (A->vpair) return GCGE_GPU_OK;
+    const size_t nz = A->nnz > 0 ? (size_t)A->nnz : 1;
+    if (cudaMalloc(&A->vpair, sizeof(float2) * nz) != cudaSuccess) {
+        A->vpair = nullptr;
+        return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
+    }
+    if (cudaMalloc(&A->pair_meta, 4 * sizeof(int)) != cudaSuccess) {
+        cudaFree(A->vpair);
+        A->vpair = nullptr;
+        A->pair_meta = nullptr;
+        return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
+    }
+    if (cudaMemsetAsync(A->pair_meta, 0, 4 * sizeof(int), ctx->stream) != cudaSuccess)
+        return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+    const int grid = ctx->num_sms * 8;
+    GB_LAUNCH(ctx, k_pair_absmax, grid, 256, 0, A->nnz, A->v, (unsigned long long *)A->pair_meta);
+    GB_LAUNCH(ctx, k_pair_vals, grid, 256, 0, A->nnz, A->v, (float2 *)A->vpair, A->pair_meta);
+    return GCGE_GPU_OK;
+}
+
+static int pair_split_x(gcge_gpu_ctx *ctx, int n, int k, const double *X, long ldx)
+{
+    const size_t need = (size_t)2 * n * k;
+    if (ctx->pairbuf_cap < need) {
+        if (ctx->pairbuf) {
+            if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+            cudaFree(ctx->pairbuf);
+            ctx->pairbuf = nullptr;
+            ctx->pairbuf_cap = 0;
+        }
+        if (cudaMalloc(&ctx->pairbuf, need * sizeof(float)) != cudaSuccess) return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
+        ctx->pairbuf_cap = need;
+    }
+    ctx->pair_epoch = ctx->pair_epoch == 0x7fffffff ? 1 : ctx->pair_epoch + 1;
+    GB_PROF(ctx, GB_K_BLAS1, 16.0 * n * k, 0.0);
+    GB_LAUNCH(ctx, k_pair_split, ctx->num_sms * 16, 256, 0, n, k, X, ldx, (float2 *)ctx->pairbuf,
+              ctx->dev_pairflag, ctx->pair_epoch);
+    return GCGE_GPU_OK;
+}
+
+#define SPMMP_CASE(LL, VV)                                                                                    \
+    if (L == LL && VW == VV) {                                                                                \
+        GB_LAUNCH(ctx, (k_spmm_pair<LL, VV>), grid, 256, 0, A->n, A->rp, A->ci, (const float2 *)A->vpair,      \
+                  A->pair_meta, (const float2 *)ctx->pairbuf, A->v, X, ldx, Y, ldy, k, ctx->dev_pairflag,       \
+                  ctx->pair_epoch);                                                                           \
+        return GCGE_GPU_OK;                                                                                   \
+    }
+#define SPMMP_L(LL) SPMMP_CASE(LL, 1) SPMMP_CASE(LL, 2) SPMMP_CASE(LL, 3) SPMMP_CASE(LL, 4) \
+    SPMMP_CASE(LL, 5) SPMMP_CASE(LL, 6) SPMMP_CASE(LL, 7) SPMMP_CASE(LL, 8)
+
+// Y = A X from the split left in ctx->pairbuf by pair_split_x
+static int spmm_pair_launch(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X, long ldx, double *Y,
+                            long ldy, int k)
+{
+    int st = pair_mat(ctx, A);
+    if (st) return st;
+    ctx->spmm_launches++;
+    GB_PROF(ctx, GB_K_SPMM64, 12.0 * A->nnz + 4.0 * (A->n + 1) + 16.0 * A->n * k, 2.0 * A->nnz * k);
+    int L = 16, VW = 4;
+    spmm64_shape(k, &L, &VW);
+    const long warps = ((long)A->n * L + 31) / 32;
+    const int grid = ceil_div_l(warps * 32, 256);
+    SPMMP_L(4)
+    SPMMP_L(8)
+    SPMMP_L(16)
+    return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+}
+
+// the products this path takes: two or more columns, Y = A X
+static bool pair_applies(const gcge_gpu_ctx *ctx, int k, double alpha, const double *alpha_col, double beta,
+                         const int *ncols_dev)
+{
+    return ctx->spmm_pair && k >= 2 && !alpha_col && beta == 0.0 && !ncols_dev && alpha == 1.0;
+}
+
+extern "C" int gb_spmm_ab(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B, const double *X,
+                          long ldx, double *YA, double *YB, long ldy, int k)
+{
+    if (k <= 0 || A->n <= 0) return GCGE_GPU_OK;
+    if (!pair_applies(ctx, k, 1.0, nullptr, 0.0, nullptr)) {
+        int st = gb_spmm(ctx, A, X, ldx, YA, ldy, k, 1.0, nullptr, 0.0, nullptr);
+        if (!st && B) st = gb_spmm(ctx, B, X, ldx, YB, ldy, k, 1.0, nullptr, 0.0, nullptr);
+        return st;
+    }
+    int st = pair_split_x(ctx, A->n, k, X, ldx);
+    if (!st) st = spmm_pair_launch(ctx, A, X, ldx, YA, ldy, k);
+    if (!st && B) st = spmm_pair_launch(ctx, B, X, ldx, YB, ldy, k);
+    return st;
+}
+
 extern "C" int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X, long ldx, double *Y,
                        long ldy, int k, double alpha, const double *alpha_col, double beta,
                        const int *ncols_dev)
 {
     if (k <= 0 || A->n <= 0) return GCGE_GPU_OK;
+    if (pair_applies(ctx, k, alpha, alpha_col, beta, ncols_dev)) {
+        int st = pair_split_x(ctx, A->n, k, X, ldx);
+        return st ? st : spmm_pair_launch(ctx, A, X, ldx, Y, ldy, k);
+    }
     ctx->spmm_launches++;
     GB_PROF(ctx, GB_K_SPMM64, 12.0 * A->nnz + 4.0 * (A->n + 1) + (beta != 0.0 ? 24.0 : 16.0) * A->n * k,
             2.0 * A->nnz * k);

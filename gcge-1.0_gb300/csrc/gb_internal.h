@@ -55,6 +55,13 @@ struct gcge_gpu_ctx {
     void *ozbuf;               /* pre-split digit planes of small operands */
     size_t ozbuf_cap;          /* bytes */
     int *dev_err;              /* device word: set by a kernel whose bounded wait ran out */
+    /* FP64 SpMM in FP32-pair arithmetic (1; set by the mixed solver form) or on the
+     * FP64 pipe (0, default) */
+    int spmm_pair;
+    float *pairbuf;            /* X split into (hi, lo) FP32 pairs */
+    size_t pairbuf_cap;        /* floats */
+    int *dev_pairflag;         /* device word: epoch of the last split that met |x| >= 2^100 */
+    int pair_epoch;
 };
 
 struct gcge_gpu_mat {
@@ -66,6 +73,8 @@ struct gcge_gpu_mat {
     double max_row_nnz;
     double *dinv;              /* 1 / diag(A) for the Jacobi preconditioner (lazy) or NULL */
     float *dinv32;             /* the same in FP32 */
+    float *vpair;              /* values x 2^-s as (hi, lo) FP32 pairs (lazy) or NULL */
+    int *pair_meta;            /* device: [0..1] max |value| bits, [2] the exponent s */
 };
 
 struct gcge_gpu_mv {
@@ -103,6 +112,9 @@ int gb_lincomb_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *X, lon
  * ncols_dev (optional): device int; columns >= *ncols_dev are left untouched. */
 int gb_spmm(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X, long ldx, double *Y, long ldy,
             int k, double alpha, const double *alpha_col, double beta, const int *ncols_dev);
+/* A X and B X (B may be NULL) from one split of X in the FP32-pair form */
+int gb_spmm_ab(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B, const double *X, long ldx,
+               double *YA, double *YB, long ldy, int k);
 int gb_spmm32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const float *X, long ldx, float *Y, long ldy,
               int k, const int *ncols_dev);
 /* y = a x + b y on an n x k block, CSR_VecAxpby special cases */

@@ -194,8 +194,7 @@ static int check_conv(gcg_t *g)
     if (nu > 0) {
         CTRY(cudaMemcpyAsync(g->unlock_d, g->unlock_h, sizeof(int) * nu, cudaMemcpyHostToDevice, ctx->stream));
         TRY(gb_gather_cols(ctx, n, nu, g->X, g->ldx, g->unlock_d, g->S1, g->lds, NULL, 0));
-        TRY(gb_spmm(ctx, g->A, g->S1, g->lds, g->S2, g->lds, nu, 1.0, NULL, 0.0, NULL));
-        if (g->B) TRY(gb_spmm(ctx, g->B, g->S1, g->lds, g->S3, g->lds, nu, 1.0, NULL, 0.0, NULL));
+        TRY(gb_spmm_ab(ctx, g->A, g->B, g->S1, g->lds, g->S2, g->S3, g->lds, nu));
         TRY(gb_residual_norms(ctx, n, nu, g->S1, g->lds, g->S2, g->lds, g->B ? g->S3 : NULL, g->lds, g->eval_d,
                               g->unlock_d, g->res_d, strcmp(g->p.conv_type, "BR") == 0));
         CTRY(cudaMemcpyAsync(g->res_h, g->res_d, sizeof(double) * 3 * nu, cudaMemcpyDeviceToHost, ctx->stream));
@@ -394,13 +393,28 @@ static void gcg_free(gcg_t *g)
 
 static int dmalloc(void **p, size_t bytes) { return cudaMalloc(p, bytes > 0 ? bytes : 8) == cudaSuccess ? 0 : 1; }
 
+static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B, const gcge_gpu_params *pin,
+                      double *eval, gcge_gpu_mv *evec, gcge_gpu_stats *stats);
+
 int GCGE_GPU_Solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B, const gcge_gpu_params *pin,
                    double *eval, gcge_gpu_mv *evec, gcge_gpu_stats *stats)
 {
     if (!ctx || !A || !pin || !eval || !evec) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     if (pin->nev <= 0 || pin->nev > A->n || evec->ncols < pin->nev || evec->n != A->n || (B && B->n != A->n) ||
-        (pin->precision && !A->v32) || pin->block_size < 0)
+        (pin->precision && !A->v32) || pin->precision < 0 || pin->precision > 2 || pin->block_size < 0)
         return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    /* precision 2: the outer products of the iteration (A W, B W, A X, B X) in
+     * FP32-pair arithmetic for the duration of this solve */
+    const int pair = ctx->spmm_pair;
+    ctx->spmm_pair = pin->precision == 2;
+    const int st = solve_impl(ctx, A, B, pin, eval, evec, stats);
+    ctx->spmm_pair = pair;
+    return st;
+}
+
+static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B, const gcge_gpu_params *pin,
+                      double *eval, gcge_gpu_mv *evec, gcge_gpu_stats *stats)
+{
     gcg_t G, *g = &G;
     memset(g, 0, sizeof(G));
     int st = 0;

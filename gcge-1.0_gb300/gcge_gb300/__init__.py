@@ -98,6 +98,7 @@ def load():
         "GCGE_GPU_ProfileEnable": (_I, [_P, _I]),
         "GCGE_GPU_ProfileRead": (_I, [_P, _I, _P, _P, _P, _P, _I]),
         "GCGE_GPU_SetTensorEmulation": (_I, [_P, _I]),
+        "GCGE_GPU_SetPairSpMM": (_I, [_P, _I]),
         "GCGE_GPU_InnerProdNoAlloc": (_I, [_I, _I, _I, _P, C.c_long, _P, C.c_long, _P, _I, _I, _P]),
         "GCGE_GPU_PatternGrad": (_I, [_P, _P, _I, _P, _I, _I, _P, _I, _P]),
         "GCGE_GPU_EigvecAdjoint": (_I, [_P, _P, _P, _I, _P, _I, _P, _I, _P, _I, _D, _D, _I, C.POINTER(_I)]),
@@ -179,6 +180,10 @@ class Context:
     def tensor_emulation(self, on):
         """Dense FP64 contractions on the tensor cores (error-free splitting) or the FP64 pipe."""
         _chk(self.lib.GCGE_GPU_SetTensorEmulation(self.h, int(on)), "SetTensorEmulation")
+
+    def pair_spmm(self, on):
+        """Sparse products with two or more columns in FP32-pair arithmetic (1) or FP64 (0)."""
+        _chk(self.lib.GCGE_GPU_SetPairSpMM(self.h, int(on)), "SetPairSpMM")
 
     def last_error(self):
         return self.lib.GCGE_GPU_GetLastError(self.h)

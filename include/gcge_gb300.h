@@ -92,6 +92,14 @@ int  GCGE_GPU_MultiVecSetRandomValue(gcge_gpu_mv *mv, int start, int nvec, unsig
  * reference (its dense work is host BLAS). */
 int  GCGE_GPU_SetTensorEmulation(gcge_gpu_ctx *ctx, int on);
 
+/* Sparse products Y = A X with two or more columns either in FP32-pair
+ * arithmetic (on = 1: values as hi + lo floats, error-free products and sums on
+ * the FP32 pipe, ~1e-14 of sum |a_ij x_j|; |x| >= 2^100 or non-finite X falls
+ * back to FP64 inside the product) or on the FP64 pipe (on = 0, the default). A
+ * solve with precision 2 switches it on for its own duration. No counterpart in
+ * the reference. */
+int  GCGE_GPU_SetPairSpMM(gcge_gpu_ctx *ctx, int on);
+
 /* ---- 2. block operations (semantics of src/gcge_ops.c:115-300) ---- */
 
 /* y(:, start[1]:end[1]) = A x(:, start[0]:end[0]); ops->MatDotMultiVec,
@@ -148,7 +156,10 @@ typedef struct {
     double orth_zero_tol;     /* 1e-16 (+DBL_EPSILON)                                 */
     char   conv_type[4];      /* "R", "A", "O" as the reference; "BR":
                                  ||Ax - lambda Bx|| / (|lambda| ||Bx||)               */
-    int    precision;         /* 0 plain FP64; 1 mixed (FP32 inner block CG)          */
+    int    precision;         /* 0 plain FP64; 1 mixed (FP32 inner block CG);
+                                 2 mixed, and the outer sparse products (A W, B W,
+                                 A X, B X) in FP32-pair arithmetic (48-bit
+                                 significand, ~1e-14 of sum |a_ij x_j|)              */
     unsigned long long seed;  /* counter-hash seed of the initial vectors             */
     int    print_level;       /* 0 silent; 1 one line per iteration (reference format)*/
     int    precond;           /* inner block CG: 0 plain (GCGE_BCG, the default);

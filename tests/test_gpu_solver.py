@@ -115,7 +115,7 @@ def check_vectors(A, B, ev, X, w_ext, Z_ext, angle=1e-7):
         assert containment_angle(X[:, mine], Z_ext[:, c], Bs) < angle, (c, ev[mine])
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 @pytest.mark.parametrize("name", sorted(GOLD))
 def test_eigenvalues_match_reference_golden(ctx, name, precision):
     """The reference's own parameters and criterion; eigenvalues against what it reported."""
@@ -123,7 +123,7 @@ def test_eigenvalues_match_reference_golden(ctx, name, precision):
     A, B = case_matrices(name)
     kw = dict(g["params"], seed=1234, precision=precision)
     kw["ev_max_it"] = max(kw.get("ev_max_it", 30), 100)
-    dA, dB = ctx.matrix(A, keep_fp32=precision == 1), (ctx.matrix(B) if B is not None else None)
+    dA, dB = ctx.matrix(A, keep_fp32=precision >= 1), (ctx.matrix(B) if B is not None else None)
     ev, X, st = ctx.solve(dA, dB, ctx.params(**kw))
     assert st.num_unlock == 0
     np.testing.assert_allclose(ev, g["eval"], rtol=1e-10, atol=0)
@@ -131,14 +131,14 @@ def test_eigenvalues_match_reference_golden(ctx, name, precision):
     assert np.all(residuals(A, B, ev, X, g["params"].get("conv_type", "R")) <= tol * 1.05)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 @pytest.mark.parametrize("name", sorted(GOLD))
 def test_eigenvectors_principal_angles(ctx, oracle, name, precision):
     g = GOLD[name]
     A, B = case_matrices(name)
     nev = g["params"]["nev"]
     kw = dict(g["params"], seed=99, precision=precision, conv_type="BR", ev_tol=1e-10, ev_max_it=300)
-    dA, dB = ctx.matrix(A, keep_fp32=precision == 1), (ctx.matrix(B) if B is not None else None)
+    dA, dB = ctx.matrix(A, keep_fp32=precision >= 1), (ctx.matrix(B) if B is not None else None)
     ev, X, st = ctx.solve(dA, dB, ctx.params(**kw))
     assert st.num_unlock == 0
     w, Z = reference_eigenspace(A, B, nev + 4, oracle)
@@ -147,7 +147,7 @@ def test_eigenvectors_principal_angles(ctx, oracle, name, precision):
     assert np.all(residuals(A, B, ev, X, "BR") <= 1.05e-10)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_laplace_analytic(ctx, precision):
     A, _ = P.laplace2d(100, 100)
     dA = ctx.matrix(A, keep_fp32=True)
@@ -158,7 +158,7 @@ def test_laplace_analytic(ctx, precision):
     assert np.all(residuals(A, None, ev, X, "BR") <= 1.05e-8)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_fem_cube_generalized_vs_dense(ctx, oracle, precision):
     A, B = P.fem_q1_cube(10)
     dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
@@ -192,13 +192,14 @@ def test_small_nev_and_blocks(ctx, nev, bs):
     assert np.max(np.abs(ev - ex) / ex) < 1e-10
 
 
-def test_varcoef3d_mixed(ctx, oracle):
+@pytest.mark.parametrize("precision", [1, 2])
+def test_varcoef3d_mixed(ctx, oracle, precision):
     """7-point variable-coefficient diffusion (exp of a sigma-1 Gaussian field, lumped
     diagonal mass U[1, 2]): the family of the 160^3 configuration at 16^3 cells."""
     A, B = P.varcoef3d(nc=16)
     dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
     ev, X, st = ctx.solve(dA, dB, ctx.params(nev=20, block_size=24, seed=8, conv_type="BR", ev_max_it=500,
-                                             precision=1))
+                                             precision=precision))
     assert st.num_unlock == 0
     oe, oX, ost = oracle.solve(A, B, oracle.params(nev=24, conv_type="BR", ev_tol=1e-11, ev_max_it=800,
                                                    init_rng=1, seed=4))
@@ -207,7 +208,7 @@ def test_varcoef3d_mixed(ctx, oracle):
     assert np.all(residuals(A, B, ev, X, "BR") <= 1.05e-8)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_jacobi_preconditioned_inner_solve(ctx, oracle, precision):
     """precond = 1 (the role of a linear solver installed in ops->LinearSolver):
     Jacobi-preconditioned block CG gives the same eigenpairs as the oracle in no
@@ -228,12 +229,13 @@ def test_jacobi_preconditioned_inner_solve(ctx, oracle, precision):
     assert its[1] <= its[0], its
 
 
-def test_irregular_graph_mixed(ctx, oracle):
+@pytest.mark.parametrize("precision", [1, 2])
+def test_irregular_graph_mixed(ctx, oracle, precision):
     """Power-law graph Laplacian (irregular rows up to 300 nonzeros), B = diag U[1,2]."""
     A, B = P.powerlaw_graph(4000, seed=11, dmax=300)
     dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
     ev, X, st = ctx.solve(dA, dB, ctx.params(nev=16, block_size=16, seed=8, conv_type="BR", ev_max_it=500,
-                                             precision=1))
+                                             precision=precision))
     assert st.num_unlock == 0
     oe, oX, ost = oracle.solve(A, B, oracle.params(nev=20, conv_type="BR", ev_tol=1e-11, ev_max_it=800,
                                                    init_rng=1, seed=4))
