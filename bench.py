@@ -42,6 +42,8 @@ WORKLOADS = {
     "fem24": (24, 20, 24),
 }
 HW_FP64_TFLOPS = 1.199   # measured FP64 FMA throughput of a GB300 (profiles/gb300_throughput_probe.md)
+HW_FP32_TOPS = 35.0      # FP32 FMA-pipe instructions per second x 1e-12 (70.0 TFLOP/s measured, same probe)
+PAIR_OPS = 13            # FP32 operations per (nonzero, column) of the FP32-pair SpMM
 
 
 def rank_env():
@@ -213,6 +215,11 @@ def roofline_from_profile(prof, hbm_peak, tensor_peak=None):
         elif fp64:
             row.update(bound="fp64", peak=HW_FP64_TFLOPS, unit="TFLOP/s", frac=tfl / HW_FP64_TFLOPS,
                        hbm_frac=gbs / hbm_peak)
+        elif cls == "spmm_pair":
+            # FP64-accurate to 48 bits on the FP32 pipe: 13 FP32 operations per (nonzero, column)
+            tops = tfl / 2.0 * PAIR_OPS
+            row.update(bound="fp32", peak=HW_FP32_TOPS, unit="Tops/s", frac=tops / HW_FP32_TOPS,
+                       achieved_fp32_tops=tops, fp64_equiv_tflops=tfl, hbm_frac=gbs / hbm_peak)
         elif cls == "dense_eig":
             row.update(bound="latency", peak=None, unit=None, frac=None)
         else:
@@ -337,9 +344,11 @@ def run_gb300(args, dist):
             "jacobi_inner_solve": jacobi,
             "gpu_launches": int(launches),
             "roofline": {"kernel": dom, "bound": d["bound"],
-                         "achieved": {"fp64": d["achieved_tflops"], "tensor": d.get("achieved_tensor_tflops")}
+                         "achieved": {"fp64": d["achieved_tflops"], "tensor": d.get("achieved_tensor_tflops"),
+                                      "fp32": d.get("achieved_fp32_tops")}
                          .get(d["bound"], d["achieved_gbs"]), "peak": d["peak"], "unit": d["unit"], "frac": d["frac"],
                          "peak_source": {"fp64": "FP64 FMA throughput measured on GB300 (profiles)",
+                                         "fp32": "FP32 FMA throughput measured on GB300 (profiles)",
                                          "tensor": "MEASURED_PEAKS.json bf16_tflops_sustained (%s)" % peak_kind}
                          .get(d["bound"], "MEASURED_PEAKS.json hbm_gbs (%s)" % peak_kind),
                          "traffic": traffic, "alg_bytes_per_launch": per_launch_alg,

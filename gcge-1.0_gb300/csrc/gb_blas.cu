@@ -299,18 +299,19 @@ __device__ __forceinline__ double pair_f2d(float f, int s)
     return __hiloint2double((int)hi, (int)((b & 7u) << 29));
 }
 
-// split an n x k block of X (leading dimension ldx) into pairs, leading dimension k
+// split an n x k block of X (leading dimension ldx) into pairs, leading dimension k:
+// blockIdx.y strides the columns in 32s, the x dimension the rows (one row per
+// thread-column group, no division)
 __global__ void __launch_bounds__(256)
 k_pair_split(int n, int k, const double *__restrict__ X, long ldx, float2 *__restrict__ Xs, int *flag, int epoch)
 {
     int bad = 0;
-    const long total = (long)n * k;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const long r = t / k;
-        const int c = (int)(t - r * k);
-        Xs[t] = pair_split(X[r * ldx + c], bad);
-    }
-    if (__any_sync(FULL, bad) && (threadIdx.x & 31) == 0) *flag = epoch;
+    const int lane = threadIdx.x & 31, c = blockIdx.y * 32 + lane;
+    const int rstride = gridDim.x * (blockDim.x >> 5);
+    if (c < k)
+        for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += rstride)
+            Xs[(long)r * k + c] = pair_split(X[(long)r * ldx + c], bad);
+    if (__any_sync(FULL, bad) && lane == 0) *flag = epoch;
 }
 
 // matrix values: max |a| (as ordered bits of a non-negative double), then the split
@@ -497,8 +498,11 @@ static int pair_split_x(gcge_gpu_ctx *ctx, int n, int k, const double *X, long l
     }
     ctx->pair_epoch = ctx->pair_epoch == 0x7fffffff ? 1 : ctx->pair_epoch + 1;
     GB_PROF(ctx, GB_K_BLAS1, 16.0 * n * k, 0.0);
-    GB_LAUNCH(ctx, k_pair_split, ctx->num_sms * 16, 256, 0, n, k, X, ldx, (float2 *)ctx->pairbuf,
-              ctx->dev_pairflag, ctx->pair_epoch);
+    const int ct = (k + 31) / 32;
+    const int gx = ceil_div_l((long)ctx->num_sms * 16, ct) < ceil_div_l(n, 8) ? ceil_div_l((long)ctx->num_sms * 16, ct)
+                                                                                : ceil_div_l(n, 8);
+    GB_LAUNCH(ctx, k_pair_split, dim3(gx, ct), 256, 0, n, k, X, ldx, (float2 *)ctx->pairbuf, ctx->dev_pairflag,
+              ctx->pair_epoch);
     return GCGE_GPU_OK;
 }
 
@@ -510,7 +514,29 @@ static int pair_split_x(gcge_gpu_ctx *ctx, int n, int k, const double *X, long l
         return GCGE_GPU_OK;                                                                                   \
     }
 #define SPMMP_L(LL) SPMMP_CASE(LL, 1) SPMMP_CASE(LL, 2) SPMMP_CASE(LL, 3) SPMMP_CASE(LL, 4) \
-    SPMMP_CASE(LL, 5) SPMMP_CASE(LL, 6) SPMMP_CASE(LL, 7) SPMMP_CASE(LL, 8)
+    SPMMP_CASE(LL, 5) SPMMP_CASE(LL, 6) SPMMP_CASE(LL, 7)
+
+// Lane shape of the pair product: the fewest idle lane slots (as for FP64);
+// among equals two columns per lane first, then the larger L. Measured on the Q1
+// cube 96^3 stiffness (us per product): k = 16: (8, 2) 355, (4, 4) 387, (16, 1)
+// 459; k = 32: (16, 2) 592, (8, 4) 640, (4, 8) 1101; k = 56: (8, 7) 852;
+// k = 64: (16, 4) 1244, (8, 8) 2140 -- eight contiguous columns per lane is a
+// slow gather pattern, so VW stops at 7.
+static void spmm_pair_shape(int k, int *Lo, int *VWo)
+{
+    double best = -1;
+    for (int L = 16; L >= 4; L >>= 1) {
+        int vw = (k + L - 1) / L;
+        if (vw > 7) vw = 7;
+        const int cols = L * vw, chunks = (k + cols - 1) / cols;
+        const double eff = (double)k / ((double)chunks * cols);
+        if (eff > best + 1e-12 || (eff > best - 1e-12 && vw == 2 && *VWo != 2)) {
+            best = eff > best ? eff : best;
+            *Lo = L;
+            *VWo = vw;
+        }
+    }
+}
 
 // Y = A X from the split left in ctx->pairbuf by pair_split_x
 static int spmm_pair_launch(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const double *X, long ldx, double *Y,
@@ -519,9 +545,9 @@ static int spmm_pair_launch(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const doub
     int st = pair_mat(ctx, A);
     if (st) return st;
     ctx->spmm_launches++;
-    GB_PROF(ctx, GB_K_SPMM64, 12.0 * A->nnz + 4.0 * (A->n + 1) + 16.0 * A->n * k, 2.0 * A->nnz * k);
-    int L = 16, VW = 4;
-    spmm64_shape(k, &L, &VW);
+    GB_PROF(ctx, GB_K_SPMMPAIR, 12.0 * A->nnz + 4.0 * (A->n + 1) + 16.0 * A->n * k, 2.0 * A->nnz * k);
+    int L = 16, VW = 0;
+    spmm_pair_shape(k, &L, &VW);
     const long warps = ((long)A->n * L + 31) / 32;
     const int grid = ceil_div_l(warps * 32, 256);
     SPMMP_L(4)

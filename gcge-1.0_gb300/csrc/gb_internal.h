@@ -23,7 +23,7 @@ extern "C" {
 #define GB_PROF_SLOTS 4096
 /* kernel classes of the profiling mode (order of GCGE_GPU_ProfileRead) */
 enum { GB_K_SPMM64, GB_K_SPMM32, GB_K_GRAM, GB_K_LINCOMB, GB_K_BCGVEC, GB_K_BLAS1, GB_K_DENSE, GB_K_EIG,
-       GB_K_REDUCE, GB_PROF_CLASSES };
+       GB_K_REDUCE, GB_K_SPMMPAIR, GB_PROF_CLASSES };
 
 struct gcge_gpu_ctx {
     int device;

@@ -120,7 +120,14 @@ __device__ __forceinline__ void tc_setup(tc_hdr *h)
 
 // MMA issue of stage s (lane 0 of the MMA warp): wait for the stage's planes
 // (and, at the first stage of a chunk, for the previous chunk's drain), issue the
-// digit pairs with p + q < LEVELS x TC_KS / 16 K steps, commit to empty[buf]
+// digit pairs with p + q < LEVELS x TC_KS / 16 K steps, commit to empty[buf].
+// The B digit planes of a stage lie back to back with the same 512-byte stride
+// between 8-row groups, and level L of the accumulator is TMEM columns 64 L ..
+// 64 L + 63, so the pairs (p, q0) .. (p, q0 + 3) are one MMA with N = 64 x 4
+// whose D starts at level p + q0: 11 MMAs per K step (10 for the Gram's seven
+// levels) instead of 34 (28), and each A plane is read from shared memory once
+// per such group instead of once per pair. The first K step of a chunk keeps
+// the pairwise order, whose first MMA into every level overwrites it.
 template <int LEVELS, bool COPIED>
 __device__ __forceinline__ void tc_issue_stage(tc_hdr *h, uint32_t sbase, uint32_t tmem, int N, int s, int cs,
                                                int *commits, int *err)
@@ -136,23 +143,39 @@ __device__ __forceinline__ void tc_issue_stage(tc_hdr *h, uint32_t sbase, uint32
         return;
     }
     tc_fence_after_sync();
+    (void)N;
     const uint32_t a0 = sbase + buf * TC_STAGE, b0 = a0 + OZ_DIGITS * TC_APLANE;
-    const uint32_t idesc = tc_idesc_f16(TC_M, N);
+    const uint32_t idesc = tc_idesc_f16(TC_M, TC_N);
 #pragma unroll
-    for (int ks = 0; ks < TC_KS / 16; ++ks)
+    for (int ks = 0; ks < TC_KS / 16; ++ks) {
+        if (cs == 0 && ks == 0) {
 #pragma unroll
-        for (int p = 0; p < OZ_DIGITS; ++p) {
-            const uint64_t ad = tc_sdesc(a0 + p * TC_APLANE + ks * 256, TC_LBO, TC_SBO);
+            for (int p = 0; p < OZ_DIGITS; ++p) {
+                const uint64_t ad = tc_sdesc(a0 + p * TC_APLANE, TC_LBO, TC_SBO);
 #pragma unroll
-            for (int q = 0; q < OZ_DIGITS; ++q) {
-                if (p + q < LEVELS) {
-                    const uint64_t bd = tc_sdesc(b0 + q * TC_BPLANE + ks * 256, TC_LBO, TC_SBO);
-                    // the first MMA into level L of a chunk is (p, q) = (max(0, L - 6), min(L, 6))
-                    const bool first = cs == 0 && ks == 0 && p == (p + q > OZ_DIGITS - 1 ? p + q - (OZ_DIGITS - 1) : 0);
-                    tc_mma_kf16(tmem + (p + q) * TC_N, ad, bd, idesc, first ? 0u : 1u);
+                for (int q = 0; q < OZ_DIGITS; ++q) {
+                    if (p + q < LEVELS) {
+                        const uint64_t bd = tc_sdesc(b0 + q * TC_BPLANE, TC_LBO, TC_SBO);
+                        // the first MMA into level L is (p, q) = (max(0, L - 6), min(L, 6))
+                        const bool first = p == (p + q > OZ_DIGITS - 1 ? p + q - (OZ_DIGITS - 1) : 0);
+                        tc_mma_kf16(tmem + (p + q) * TC_N, ad, bd, idesc, first ? 0u : 1u);
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int p = 0; p < OZ_DIGITS; ++p) {
+                const int qmax = (LEVELS - 1 - p < OZ_DIGITS - 1) ? LEVELS - 1 - p : OZ_DIGITS - 1;
+                const uint64_t ad = tc_sdesc(a0 + p * TC_APLANE + ks * 256, TC_LBO, TC_SBO);
+#pragma unroll
+                for (int q0 = 0; q0 <= qmax; q0 += 4) {
+                    const int nq = qmax - q0 + 1 < 4 ? qmax - q0 + 1 : 4;
+                    const uint64_t bd = tc_sdesc(b0 + q0 * TC_BPLANE + ks * 256, TC_LBO, TC_SBO);
+                    tc_mma_kf16(tmem + (p + q0) * TC_N, ad, bd, tc_idesc_f16(TC_M, TC_N * nq), 1u);
                 }
             }
         }
+    }
     tc_mma_commit(empty);
     ++commits[buf];
 }
@@ -720,7 +743,7 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
                             long long a, b;
                             oz_levels_to_int<LC_LEVELS>(lev, a, b);
                             const double d =
-                                oz_to_double<40>(a, b, my_e + ecs[col0 + g4 * 4 + q] - OZ_SCALE_OFFSET);
+                                oz_to_double40(a, b, my_e + ecs[col0 + g4 * 4 + q] - OZ_SCALE_OFFSET);
                             double v2 = d;
                             if (MULTI) {
                                 acc[g4 * 4 + q] = first ? d : acc[g4 * 4 + q] + d;

@@ -183,44 +183,7 @@ __device__ __forceinline__ uint32_t oz_pack(unsigned long long u0, unsigned long
     return r;
 }
 
-// ---------------------------------------------------------------- exact integer -> FP64
-// (hi 2^SH + lo) 2^(s - 16 - SH) rounded once to nearest-even, s = e + f -
-// OZ_SCALE_OFFSET: hi holds levels 0-2 in units of 2^-16, lo the lower levels in
-// units of 2^-(16 + SH) (SH = 32 for levels 3-6, 40 for levels 3-7)
-template <int SH>
-__device__ __forceinline__ double oz_to_double(long long hi, long long lo, int s)
-{
-    __int128 z = ((__int128)hi << SH) + (__int128)lo;
-    if (z == 0) return 0.0;
-    unsigned long long sign = 0;
-    if (z < 0) {
-        sign = 1ull << 63;
-        z = -z;
-    }
-    const unsigned __int128 u = (unsigned __int128)z;
-    const unsigned long long zh = (unsigned long long)(u >> 64), zl = (unsigned long long)u;
-    const int nb = zh ? 128 - __clzll((long long)zh) : 64 - __clzll((long long)zl);
-    int E = nb - 1 + s - 16 - SH;
-    unsigned long long m;
-    if (nb <= 53) {
-        m = zl << (53 - nb);
-    } else {
-        const int sh = nb - 53;
-        const unsigned __int128 q = u >> sh;
-        const unsigned __int128 rem = u - (q << sh);
-        const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
-        m = (unsigned long long)q;
-        if (rem > half || (rem == half && (m & 1))) ++m;
-        if (m >> 53) {
-            m >>= 1;
-            ++E;
-        }
-    }
-    if (E < -1022 || E > 1023)                     // outside the normal range: scale in FP64
-        return ldexp((double)hi, s - 16) + ldexp((double)lo, s - 16 - SH);
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(E + 1023) << 52) |
-                                            (m & ((1ull << 52) - 1))));
-}
+#include "gb_ozconv.h"
 
 // levels (exact FP32 integers) -> hi (levels 0-2, units 2^-16) and lo (levels
 // 3 .. LEVELS-1 in units of the lowest level) of one output

@@ -192,7 +192,7 @@ class Context:
         return self.lib.GCGE_GPU_LaunchCount(self.h)
 
     PROFILE_CLASSES = ("spmm_fp64", "spmm_fp32", "gram", "lincomb", "bcg_vec", "blas1", "dense_gemm",
-                       "dense_eig", "reduce")
+                       "dense_eig", "reduce", "spmm_pair")
 
     def profile(self, on):
         _chk(self.lib.GCGE_GPU_ProfileEnable(self.h, int(on)), "ProfileEnable")

@@ -208,7 +208,8 @@ long long GCGE_GPU_LaunchCount(const gcge_gpu_ctx *ctx);
  * stream and attributed to a class with its algorithmic bytes and flops.
  * Classes, in order: 0 CSR SpMM FP64, 1 CSR SpMM FP32, 2 Gram V^T W,
  * 3 linear combination X*C, 4 block-CG vector updates and dots, 5 AXPBY/copies,
- * 6 small dense GEMM, 7 small dense eigensolve, 8 per-column reductions.
+ * 6 small dense GEMM, 7 small dense eigensolve, 8 per-column reductions,
+ * 9 CSR SpMM in FP32-pair arithmetic.
  * ProfileRead fills up to nclass entries of each non-NULL array and returns
  * the number of classes (reset != 0 zeroes the totals afterwards). */
 int  GCGE_GPU_ProfileEnable(gcge_gpu_ctx *ctx, int on);
