@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libgcge_gb300.so")
 OBJ = os.path.join(HERE, "_build")
 CU = ["gb_blas.cu", "gb_bcg.cu", "gb_dense.cu", "gb_api.cu", "gb_noalloc.cu", "gb_ozaki.cu", "gb_adjoint.cu"]
-C = ["gb_solver.c", "gb_ops_table.c"]
+C = ["gb_solver.c", "gb_ops_table.c", "gb_csrio.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

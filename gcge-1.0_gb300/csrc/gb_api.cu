@@ -201,6 +201,7 @@ extern "C" const char *GCGE_GPU_ErrorString(int st)
     case GCGE_GPU_ERR_BREAKDOWN: return "orthogonalisation lost every column";
     case GCGE_GPU_ERR_EIGSOLVE: return "projected eigensolve failed";
     case GCGE_GPU_ERR_TIMEOUT: return "tensor-core kernel wait timed out";
+    case GCGE_GPU_ERR_IO: return "file missing, unreadable, truncated or not CSR";
     default: return "unknown status";
     }
 }

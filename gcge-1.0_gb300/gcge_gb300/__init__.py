@@ -17,9 +17,11 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(_HERE), "libgcge_gb300.so")
 
 OK = 0
+ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_CSR, ERR_NONFINITE, ERR_BREAKDOWN, ERR_EIGSOLVE, ERR_TIMEOUT, ERR_IO = range(1, 10)
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "device allocation failed",
           4: "malformed CSR matrix", 5: "non-finite value", 6: "orthogonalisation lost every column",
-          7: "projected eigensolve failed"}
+          7: "projected eigensolve failed", 8: "tensor-core kernel wait timed out",
+          9: "file missing, unreadable, truncated or not CSR"}
 
 
 class GcgeGpuError(RuntimeError):
@@ -102,6 +104,15 @@ def load():
         "GCGE_GPU_InnerProdNoAlloc": (_I, [_I, _I, _I, _P, C.c_long, _P, C.c_long, _P, _I, _I, _P]),
         "GCGE_GPU_PatternGrad": (_I, [_P, _P, _I, _P, _I, _I, _P, _I, _P]),
         "GCGE_GPU_EigvecAdjoint": (_I, [_P, _P, _P, _I, _P, _I, _P, _I, _P, _I, _D, _D, _I, C.POINTER(_I)]),
+        "GCGE_GPU_CSRReadText": (_I, [C.c_char_p, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I),
+                                      C.POINTER(C.POINTER(_I)), C.POINTER(C.POINTER(_I)),
+                                      C.POINTER(C.POINTER(_D))]),
+        "GCGE_GPU_CSRReadBinary": (_I, [C.c_char_p, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I),
+                                        C.POINTER(C.POINTER(_I)), C.POINTER(C.POINTER(_I)),
+                                        C.POINTER(C.POINTER(_D))]),
+        "GCGE_GPU_CSRWriteBinary": (_I, [C.c_char_p, _I, _I, _I, _P, _P, _P]),
+        "GCGE_GPU_CSRFree": (None, [C.POINTER(_I), C.POINTER(_I), C.POINTER(_D)]),
+        "GCGE_GPU_MatCreateFromFile": (_I, [_P, C.c_char_p, _I, C.POINTER(_P)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -210,6 +221,10 @@ class Context:
     def matrix(self, csr, keep_fp32=False):
         return Matrix(self, csr, keep_fp32)
 
+    def matrix_from_file(self, path, keep_fp32=False):
+        """Read a CSR file (the reference's text format or the binary form) and upload it."""
+        return Matrix(self, None, keep_fp32, path=path)
+
     def multivec(self, n, k, data=None):
         mv = MultiVec(self, n, k)
         if data is not None:
@@ -258,8 +273,19 @@ class Context:
 
 
 class Matrix:
-    def __init__(self, ctx, csr, keep_fp32=False):
+    def __init__(self, ctx, csr, keep_fp32=False, path=None):
         self.ctx, self.lib = ctx, ctx.lib
+        if path is not None:
+            # read and upload in the library (GCGE_GPU_MatCreateFromFile): text or binary
+            h = _P()
+            _chk(self.lib.GCGE_GPU_MatCreateFromFile(ctx.h, os.fsencode(path), int(keep_fp32), C.byref(h)),
+                 "GCGE_GPU_MatCreateFromFile")
+            self.h = h
+            n, nnz = _I(), _I()
+            _chk(self.lib.GCGE_GPU_MatGetSize(h, C.byref(n), C.byref(nnz)), "GCGE_GPU_MatGetSize")
+            self.n = n.value
+            ctx._adopt(self)
+            return
         self.n = csr.n
         self._rp, self._ci, self._v = _arr(csr.rowptr, np.int32), _arr(csr.col, np.int32), _arr(csr.val, np.float64)
         h = _P()
@@ -375,3 +401,31 @@ def orthonormalize(W, start, end, B=None, max_reorth_time=3, orth_zero_tol=1e-16
     _chk(W.lib.GCGE_GPU_Orthonormalize(W.h, start, C.byref(e), B.h if B is not None else None, max_reorth_time,
                                        orth_zero_tol), "Orthonormalize")
     return e.value
+
+
+def read_csr(path, binary=False):
+    """A CSR file read by the library (GCGE_GPU_CSRReadText / CSRReadBinary), as problems.CSR."""
+    from .problems import CSR
+    L = load()
+    nr, nc, nz = _I(), _I(), _I()
+    rp, ci, v = C.POINTER(_I)(), C.POINTER(_I)(), C.POINTER(_D)()
+    f = L.GCGE_GPU_CSRReadBinary if binary else L.GCGE_GPU_CSRReadText
+    _chk(f(os.fsencode(path), C.byref(nr), C.byref(nc), C.byref(nz), C.byref(rp), C.byref(ci), C.byref(v)),
+         "GCGE_GPU_CSRRead")
+    try:
+        rowptr = np.ctypeslib.as_array(rp, shape=(nr.value + 1,)).astype(np.int64)
+        col = np.ctypeslib.as_array(ci, shape=(max(nz.value, 1),))[:nz.value].astype(np.int64)
+        val = np.ctypeslib.as_array(v, shape=(max(nz.value, 1),))[:nz.value].copy()
+    finally:
+        L.GCGE_GPU_CSRFree(rp, ci, v)
+    if nr.value != nc.value:
+        raise ValueError("square matrices only (%d x %d)" % (nr.value, nc.value))
+    return CSR(rowptr, col, val)
+
+
+def write_csr_binary(path, csr):
+    """Write the binary CSR form (GCGE_GPU_CSRWriteBinary)."""
+    L = load()
+    rp, ci, v = _arr(csr.rowptr, np.int32), _arr(csr.col, np.int32), _arr(csr.val, np.float64)
+    _chk(L.GCGE_GPU_CSRWriteBinary(os.fsencode(path), csr.n, csr.n, len(v), _ptr(rp), _ptr(ci), _ptr(v)),
+         "GCGE_GPU_CSRWriteBinary")

@@ -48,6 +48,7 @@ extern "C" {
 #define GCGE_GPU_ERR_BREAKDOWN 6   /* orthogonalisation lost every column               */
 #define GCGE_GPU_ERR_EIGSOLVE  7   /* projected eigensolve did not converge             */
 #define GCGE_GPU_ERR_TIMEOUT   8   /* a tensor-core kernel's bounded wait ran out       */
+#define GCGE_GPU_ERR_IO        9   /* file missing, unreadable, truncated or not CSR    */
 
 typedef struct gcge_gpu_ctx gcge_gpu_ctx;  /* device, stream, reduction scratch  */
 typedef struct gcge_gpu_mat gcge_gpu_mat;  /* CSR matrix resident in HBM         */
@@ -75,6 +76,24 @@ int  GCGE_GPU_MatCreate(gcge_gpu_ctx *ctx, int n, const int *rowptr, const int *
 int  GCGE_GPU_MatSetValues(gcge_gpu_mat *A, const double *val);
 int  GCGE_GPU_MatDestroy(gcge_gpu_mat *A);
 int  GCGE_GPU_MatGetSize(const gcge_gpu_mat *A, int *n, int *nnz);
+
+/* CSR files (host only, no device needed). Text: the reference's format
+ * (CSR_ReadMatFile, app/csr/gcge_app_csr.c:185-236): nrow, ncol, nnz, RowPtr[nrow+1],
+ * KCol[nnz], Entries[nnz], white-space separated, 0-based; a failure returns a
+ * status (GCGE_GPU_ERR_IO, GCGE_GPU_ERR_CSR) where the reference exits. Binary:
+ * "GCGECSR\1", int32 nrow, int32 ncol, int64 nnz, then the three arrays (int32,
+ * int32, float64), little endian. The readers allocate the arrays; release them
+ * with GCGE_GPU_CSRFree. MatCreateFromFile reads either form (by the header) and
+ * uploads it (square matrices), the reading part of GCGE_CSR_Solver_Init
+ * (app/csr/gcge_app_csr.c:92-124). */
+int  GCGE_GPU_CSRReadText(const char *path, int *nrow, int *ncol, int *nnz, int **rowptr, int **col,
+                          double **val);
+int  GCGE_GPU_CSRReadBinary(const char *path, int *nrow, int *ncol, int *nnz, int **rowptr, int **col,
+                            double **val);
+int  GCGE_GPU_CSRWriteBinary(const char *path, int nrow, int ncol, int nnz, const int *rowptr, const int *col,
+                             const double *val);
+void GCGE_GPU_CSRFree(int *rowptr, int *col, double *val);
+int  GCGE_GPU_MatCreateFromFile(gcge_gpu_ctx *ctx, const char *path, int keep_fp32, gcge_gpu_mat **A);
 
 int  GCGE_GPU_MultiVecCreate(gcge_gpu_ctx *ctx, int n, int ncols, gcge_gpu_mv **mv);
 int  GCGE_GPU_MultiVecDestroy(gcge_gpu_mv *mv);

@@ -241,3 +241,25 @@ def test_irregular_graph_mixed(ctx, oracle, precision):
                                                    init_rng=1, seed=4))
     assert np.max(np.abs(ev - oe[:16]) / np.abs(oe[:16])) < 1e-9
     assert np.all(residuals(A, B, ev, X, "BR") <= 1.05e-8)
+
+
+@pytest.mark.parametrize("form", ["text", "binary"])
+def test_reference_pencil_from_file(ctx, tmp_path, form):
+    """The reference's A_5/M_5 pencil written out in its text CSR layout (and in
+    the binary form), read and uploaded by GCGE_GPU_MatCreateFromFile, solved with
+    the reference's parameters: eigenvalues within 1e-10 of what it reported."""
+    from test_csrio import write_text
+    g = GOLD["fem33_nev10_dirichlet"]
+    A, B = case_matrices("fem33_nev10_dirichlet")
+    paths = []
+    for name, M in (("A_5", A), ("M_5", B)):
+        p = str(tmp_path / (name + (".txt" if form == "text" else ".bin")))
+        write_text(p, M) if form == "text" else G.write_csr_binary(p, M)
+        paths.append(p)
+    dA, dB = ctx.matrix_from_file(paths[0]), ctx.matrix_from_file(paths[1])
+    assert dA.n == A.n
+    kw = dict(g["params"], seed=1234)
+    kw["ev_max_it"] = max(kw.get("ev_max_it", 30), 100)
+    ev, X, st = ctx.solve(dA, dB, ctx.params(**kw))
+    assert st.num_unlock == 0
+    np.testing.assert_allclose(ev, g["eval"], rtol=1e-10, atol=0)
