@@ -655,7 +655,10 @@ extern "C" int gb_orth_ws_alloc(gcge_gpu_ctx *ctx, gb_orth_ws *ws, int n, int ma
         cudaMalloc(&ws->Cm, sizeof(double) * ((size_t)max_start + max_width) * max_width) != cudaSuccess ||
         cudaMalloc(&ws->chol_work, sizeof(double) * 2 * kk) != cudaSuccess ||
         cudaMalloc(&ws->small, sizeof(double) * 64) != cudaSuccess ||
-        cudaMalloc(&ws->kept_dev, sizeof(int) * 4) != cudaSuccess) {
+        cudaMalloc(&ws->kept_dev, sizeof(int) * 4) != cudaSuccess ||
+        cudaMalloc(&ws->ev_work, sizeof(double) * gb_syevx_work_doubles(max_width)) != cudaSuccess ||
+        cudaMalloc(&ws->ev_val, sizeof(double) * max_width) != cudaSuccess ||
+        cudaMalloc(&ws->ev_info, sizeof(int) * 4) != cudaSuccess) {
         gb_orth_ws_free(ws);
         return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
     }
@@ -671,6 +674,9 @@ extern "C" void gb_orth_ws_free(gb_orth_ws *ws)
     if (ws->chol_work) cudaFree(ws->chol_work);
     if (ws->small) cudaFree(ws->small);
     if (ws->kept_dev) cudaFree(ws->kept_dev);
+    if (ws->ev_work) cudaFree(ws->ev_work);
+    if (ws->ev_val) cudaFree(ws->ev_val);
+    if (ws->ev_info) cudaFree(ws->ev_info);
     memset(ws, 0, sizeof(*ws));
 }
 
@@ -795,6 +801,177 @@ extern "C" int gb_orthonormalize(gcge_gpu_ctx *ctx, int n, double *V, long ldv, 
     if ((st = cholqr2(ctx, n, W, ldv, &k, B, zero_tol, ws))) return st;
     *end = start + k;
     return GCGE_GPU_OK;
+}
+
+// ---------------------------------------------------------------- orthonormalisation variants
+extern "C" int gb_orth_kind(const char *t)
+{
+    if (!t || !t[0] || strcmp(t, "multi") == 0) return GB_ORTH_MULTI;
+    if (strcmp(t, "cbgs") == 0) return GB_ORTH_CBGS;
+    if (strcmp(t, "scbgs") == 0) return GB_ORTH_SCBGS;
+    return GB_ORTH_GS;                                   // "bgs" and the reference's fallback branch
+}
+
+// T[:, 0:kept) = Q[:, f:k) diag(theta[f:k])^-1/2 with f one past the last
+// eigenvalue below the tolerance (ascending theta; the reference's
+// tmp_eval_nonzero_start), kept = k - f; one block. A direction is kept when
+// its norm sqrt(theta) exceeds the zero tolerance and theta exceeds 1e-12 of the
+// largest eigenvalue -- the two tests of the Cholesky-QR form on its pivots (the
+// eigensolver resolves theta only to ~1e-16 theta_max)
+__global__ void k_eig_inv_sqrt(int k, const double *__restrict__ Q, int ldq, const double *__restrict__ theta,
+                               double tol, double *__restrict__ T, int ldt, int *__restrict__ kept)
+{
+    __shared__ int f;
+    if (threadIdx.x == 0) {
+        const double rel = theta[k - 1] > 0.0 ? 1e-12 * theta[k - 1] : 0.0;
+        int s = 0;
+        for (int j = 0; j < k; ++j)
+            if (!(theta[j] > tol * tol && theta[j] > rel)) s = j + 1;
+        f = s;
+        *kept = k - s;
+    }
+    __syncthreads();
+    const int kp = k - f;
+    for (int e = threadIdx.x; e < k * kp; e += blockDim.x) {
+        const int i = e % k, c = e / k;
+        T[i + (long)c * ldt] = Q[i + (long)(c + f) * ldq] / sqrt(theta[c + f]);
+    }
+}
+
+// one eigenvalue step of W (k columns): W <- W Q theta^-1/2; *k shrinks by the dropped columns
+static int eig_orth(gcge_gpu_ctx *ctx, int n, double *W, long ldw, int *k_io, const gcge_gpu_mat *B, double zero_tol,
+                    gb_orth_ws *ws)
+{
+    const int k = *k_io;
+    const double *BW = W;
+    long ldbw = ldw;
+    int st;
+    if (B) {
+        if ((st = gb_spmm(ctx, B, W, ldw, ws->T1, ws->ld1, k, 1.0, nullptr, 0.0, nullptr))) return st;
+        BW = ws->T1;
+        ldbw = ws->ld1;
+    }
+    if ((st = gb_gram(ctx, n, k, k, W, ldw, BW, ldbw, ws->G, k, 1))) return st;
+    if ((st = gb_syevx(ctx, k, ws->G, k, 1, k, ws->ev_val, ws->Tm, k, ws->ev_work, ws->ev_info))) return st;
+    GB_LAUNCH(ctx, k_eig_inv_sqrt, 1, 256, 0, k, ws->Tm, k, ws->ev_val, zero_tol, ws->Cm, k, ws->kept_dev);
+    int h[2] = {0, 0};
+    CUDA_TRY(ctx, cudaMemcpyAsync(h, ws->kept_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpyAsync(h + 1, ws->ev_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h[1]) return gb_fail(ctx, GCGE_GPU_ERR_EIGSOLVE);
+    const int kept = h[0];
+    if (kept <= 0) {
+        *k_io = 0;
+        return GCGE_GPU_OK;
+    }
+    if ((st = gb_lincomb(ctx, n, k, kept, W, ldw, ws->Cm, k, 1.0, 0.0, ws->T1, ws->ld1, 0))) return st;
+    if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldw))) return st;
+    *k_io = kept;
+    return GCGE_GPU_OK;
+}
+
+// block projection W -= V (V^T B W), V = the first `start` columns
+static int block_project(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int k, const gcge_gpu_mat *B,
+                         gb_orth_ws *ws)
+{
+    double *W = V + start;
+    const double *BW = W;
+    long ldbw = ldv;
+    int st;
+    if (B) {
+        if ((st = gb_spmm(ctx, B, W, ldv, ws->T1, ws->ld1, k, 1.0, nullptr, 0.0, nullptr))) return st;
+        BW = ws->T1;
+        ldbw = ws->ld1;
+    }
+    if ((st = gb_gram(ctx, n, start, k, V, ldv, BW, ldbw, ws->G, start, 0))) return st;
+    return gb_lincomb(ctx, n, start, k, V, ldv, ws->G, start, -1.0, 1.0, W, ldv, 0);
+}
+
+// column-by-column Gram-Schmidt in the B inner product, two projections per
+// column; a column whose B-norm falls to the zero tolerance, or whose squared
+// B-norm to 1e-24 of its value before the projections, is replaced by the last one
+static int gs_orth(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int *end, const gcge_gpu_mat *B,
+                   double zero_tol, gb_orth_ws *ws)
+{
+    int k = *end - start, st;
+    auto bnorm2 = [&](int col, double *out) -> int {
+        const double *bw = V + col;
+        long ld = ldv;
+        int s;
+        if (B) {
+            if ((s = gb_spmm(ctx, B, V + col, ldv, ws->T1, ws->ld1, 1, 1.0, nullptr, 0.0, nullptr))) return s;
+            bw = ws->T1;
+            ld = ws->ld1;
+        }
+        if ((s = gb_gram(ctx, n, 1, 1, V + col, ldv, bw, ld, ws->small, 1, 0))) return s;
+        CUDA_TRY(ctx, cudaMemcpyAsync(out, ws->small, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        return GCGE_GPU_OK;
+    };
+    for (int j = 0; j < k;) {
+        const int col = start + j;
+        double before = 0.0, after = 0.0;
+        if ((st = bnorm2(col, &before))) return st;
+        for (int pass = 0; pass < 2 && col > 0; ++pass) {
+            const double *bw = V + col;
+            long ld = ldv;
+            if (B) {
+                if ((st = gb_spmm(ctx, B, V + col, ldv, ws->T1, ws->ld1, 1, 1.0, nullptr, 0.0, nullptr))) return st;
+                bw = ws->T1;
+                ld = ws->ld1;
+            }
+            if ((st = gb_gram(ctx, n, col, 1, V, ldv, bw, ld, ws->G, col, 0))) return st;
+            if ((st = gb_lincomb(ctx, n, col, 1, V, ldv, ws->G, col, -1.0, 1.0, V + col, ldv, 0))) return st;
+        }
+        if ((st = bnorm2(col, &after))) return st;
+        if (!(sqrt(after) > zero_tol) || !(after > 1e-24 * before)) {
+            // dependent column: the last unprocessed column takes its place
+            if (j != k - 1 && (st = gb_axpby(ctx, n, 1, 1.0, V + start + k - 1, ldv, 0.0, V + col, ldv))) return st;
+            --k;
+            continue;
+        }
+        if ((st = gb_axpby(ctx, n, 1, 1.0 / sqrt(after), V + col, ldv, 0.0, V + col, ldv))) return st;
+        ++j;
+    }
+    *end = start + k;
+    return GCGE_GPU_OK;
+}
+
+extern "C" int gb_orthonormalize_kind(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int *end,
+                                      const gcge_gpu_mat *B, int max_reorth_time, double zero_tol, gb_orth_ws *ws,
+                                      int kind)
+{
+    if (kind == GB_ORTH_MULTI) return gb_orthonormalize(ctx, n, V, ldv, start, end, B, max_reorth_time, zero_tol, ws);
+    int k = *end - start;
+    if (k <= 0) return GCGE_GPU_OK;
+    if (k > ws->max_width || start > ws->max_start || ((size_t)start + k) * k > ws->g_cap)
+        return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    if (kind == GB_ORTH_GS) return gs_orth(ctx, n, V, ldv, start, end, B, zero_tol, ws);
+    int st;
+    if (start > 0)
+        for (int pass = 0; pass < 2; ++pass)
+            if ((st = block_project(ctx, n, V, ldv, start, k, B, ws))) return st;
+    const int rounds = kind == GB_ORTH_SCBGS ? 2 : 1;
+    for (int r = 0; r < rounds && k > 0; ++r)
+        if ((st = eig_orth(ctx, n, V + start, ldv, &k, B, zero_tol, ws))) return st;
+    *end = start + k;
+    return GCGE_GPU_OK;
+}
+
+extern "C" int GCGE_GPU_OrthonormalizeType(gcge_gpu_mv *W, int start, int *end, const gcge_gpu_mat *B,
+                                           int max_reorth_time, double orth_zero_tol, const char *w_orth_type)
+{
+    if (!W || !end || start < 0 || *end < start || *end > W->ncols || (B && B->n != W->n))
+        return gb_fail(W ? W->ctx : nullptr, GCGE_GPU_ERR_ARG);
+    gcge_gpu_ctx *ctx = W->ctx;
+    gb_orth_ws ws;
+    int st = gb_orth_ws_alloc(ctx, &ws, W->n, *end - start > 0 ? *end - start : 1, start);
+    if (st) return st;
+    st = gb_orthonormalize_kind(ctx, W->n, W->d, W->ld, start, end, B, max_reorth_time, orth_zero_tol + DBL_EPSILON,
+                                &ws, gb_orth_kind(w_orth_type));
+    cudaStreamSynchronize(ctx->stream);
+    gb_orth_ws_free(&ws);
+    return st;
 }
 
 extern "C" int GCGE_GPU_Orthonormalize(gcge_gpu_mv *W, int start, int *end, const gcge_gpu_mat *B, int max_reorth_time,

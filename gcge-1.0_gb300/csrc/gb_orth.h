@@ -22,7 +22,14 @@ typedef struct {
     double *chol_work;
     double *small;   /* norms */
     int *kept_dev;
+    double *ev_work; /* eigensolve of a max_width Gram (w_orth_type cbgs / scbgs) */
+    double *ev_val;
+    int *ev_info;
 } gb_orth_ws;
+
+/* W-orthonormalisation variants (w_orth_type, src/gcge_eigsol.c:448-472) */
+enum { GB_ORTH_MULTI = 0, GB_ORTH_CBGS = 1, GB_ORTH_SCBGS = 2, GB_ORTH_GS = 3 };
+int gb_orth_kind(const char *w_orth_type);
 
 int  gb_orth_ws_alloc(gcge_gpu_ctx *ctx, gb_orth_ws *ws, int n, int max_width, int max_start);
 void gb_orth_ws_free(gb_orth_ws *ws);
@@ -35,6 +42,17 @@ void gb_orth_ws_free(gb_orth_ws *ws);
  * Cholesky-QR reuses the second pass's B product (see gb_api.cu). */
 int gb_orthonormalize(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int *end,
                       const gcge_gpu_mat *B, int max_reorth_time, double zero_tol, gb_orth_ws *ws);
+
+/* the same contract by the variant `kind`: GB_ORTH_MULTI is gb_orthonormalize;
+ * CBGS two block projection passes, then W <- W Q diag(theta)^-1/2 from the
+ * eigenpairs (theta, Q) of W^T B W, dropping theta below the zero tolerance
+ * (GCGE_CBOrthonormalization, src/gcge_orthogonal.c:755-964); SCBGS the same
+ * with the eigenvalue step repeated once to repair its rounding
+ * (GCGE_SCBOrthonormalization, :967-1279); GS column by column, two projections
+ * of each column against every column before it, then its B-norm
+ * (GCGE_BOrthonormalization :352-528 and GCGE_Orthonormalization :112-305). */
+int gb_orthonormalize_kind(gcge_gpu_ctx *ctx, int n, double *V, long ldv, int start, int *end,
+                           const gcge_gpu_mat *B, int max_reorth_time, double zero_tol, gb_orth_ws *ws, int kind);
 
 /* column-major host n x k  <->  row-major device block columns */
 int gb_upload_cols(gcge_gpu_ctx *ctx, int n, int k, const double *host, double *d, long ld);

@@ -71,6 +71,7 @@ typedef struct {
     /* state (GCGE_WORKSPACE / GCGE_PARA members) */
     int dim_x, dim_xp, dim_xpw, last_dim_xpw, last_dim_x, unconv_bs, num_unlock, num_iter;
     double max_res, min_res, sum_res, conv_omega_norm, zero_tol;
+    int orth_kind;             /* w_orth_type variant (gb_orth.h) */
     gb_orth_ws ows;
     phase_timer tm;
 } gcg_t;
@@ -128,6 +129,7 @@ void GCGE_GPU_ParamsDefault(gcge_gpu_params *p)
     p->cg_rate = 1e-2;
     p->orth_zero_tol = 1e-16;
     strcpy(p->conv_type, "R");
+    strcpy(p->w_orth_type, "multi");
     p->precision = 0;
     p->seed = 1;
 }
@@ -426,6 +428,8 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
     g->nev = pin->nev;
     g->bs = pin->block_size ? pin->block_size : pin->nev;
     g->zero_tol = pin->orth_zero_tol + DBL_EPSILON;
+    g->p.w_orth_type[sizeof(g->p.w_orth_type) - 1] = '\0';
+    g->orth_kind = gb_orth_kind(g->p.w_orth_type);
     const int nev = g->nev, n = g->n;
     /* GCGE_WORKSPACE_Setup sizes (src/gcge_workspace.c:61-73) */
     {
@@ -551,7 +555,8 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
     g->last_dim_xpw = g->dim_xpw;
     g->dim_xpw = g->dim_xp + g->unconv_bs;
     ph_begin(g, PH_W_ORTH);
-    TRY(gb_orthonormalize(ctx, n, g->V, g->ldv, g->dim_x, &g->dim_xpw, B, g->p.max_reorth_time, g->zero_tol, &g->ows));
+    TRY(gb_orthonormalize_kind(ctx, n, g->V, g->ldv, g->dim_x, &g->dim_xpw, B, g->p.max_reorth_time, g->zero_tol,
+                               &g->ows, g->orth_kind));
     ph_end(g);
     g->dim_xp = nev;
     ph_begin(g, PH_RR_MAT);
@@ -579,8 +584,8 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
             g->last_dim_xpw = g->dim_xpw;
             g->dim_xpw = g->dim_xp + g->unconv_bs;
             ph_begin(g, PH_W_ORTH);
-            TRY(gb_orthonormalize(ctx, n, g->V, g->ldv, g->dim_xp, &g->dim_xpw, B, g->p.max_reorth_time, g->zero_tol,
-                                  &g->ows));
+            TRY(gb_orthonormalize_kind(ctx, n, g->V, g->ldv, g->dim_xp, &g->dim_xpw, B, g->p.max_reorth_time,
+                                       g->zero_tol, &g->ows, g->orth_kind));
             ph_end(g);
             ph_begin(g, PH_RR_MAT);
             TRY(rr_matrix(g));

@@ -35,7 +35,7 @@ class Params(C.Structure):
                 ("max_reorth_time", C.c_int), ("dirichlet_boundary", C.c_int), ("given_init_evec", C.c_int),
                 ("ev_tol", C.c_double), ("cg_rate", C.c_double), ("orth_zero_tol", C.c_double),
                 ("conv_type", C.c_char * 4), ("precision", C.c_int), ("seed", C.c_ulonglong),
-                ("print_level", C.c_int), ("precond", C.c_int)]
+                ("print_level", C.c_int), ("precond", C.c_int), ("w_orth_type", C.c_char * 8)]
 
 
 class Stats(C.Structure):
@@ -89,6 +89,7 @@ def load():
         "GCGE_GPU_MultiVecSwap": (_I, [_P, _P, _P, _P]),
         "GCGE_GPU_BCG": (_I, [_P, _P, _I, _P, _I, _I, _I, _D, _I]),
         "GCGE_GPU_Orthonormalize": (_I, [_P, _I, C.POINTER(_I), _P, _I, _D]),
+        "GCGE_GPU_OrthonormalizeType": (_I, [_P, _I, C.POINTER(_I), _P, _I, _D, C.c_char_p]),
         "GCGE_GPU_ParamsDefault": (None, [C.POINTER(Params)]),
         "GCGE_GPU_Solve": (_I, [_P, _P, _P, C.POINTER(Params), _P, _P, C.POINTER(Stats)]),
         "GCGE_GPU_SolveHost": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, C.POINTER(Params), _P, _P, C.POINTER(Stats)]),
@@ -236,7 +237,7 @@ class Context:
         p = Params()
         self.lib.GCGE_GPU_ParamsDefault(C.byref(p))
         for k, v in kw.items():
-            if k == "conv_type":
+            if k in ("conv_type", "w_orth_type"):
                 v = v.encode()
             setattr(p, k, v)
         return p
@@ -396,10 +397,15 @@ def eigvec_adjoint(A, B, X, m, eval_, k, G, g_col, MU, mu_col, cluster_tol=1e-10
     return it.value
 
 
-def orthonormalize(W, start, end, B=None, max_reorth_time=3, orth_zero_tol=1e-16):
+def orthonormalize(W, start, end, B=None, max_reorth_time=3, orth_zero_tol=1e-16, w_orth_type=None):
     e = C.c_int(end)
-    _chk(W.lib.GCGE_GPU_Orthonormalize(W.h, start, C.byref(e), B.h if B is not None else None, max_reorth_time,
-                                       orth_zero_tol), "Orthonormalize")
+    if w_orth_type is None:
+        _chk(W.lib.GCGE_GPU_Orthonormalize(W.h, start, C.byref(e), B.h if B is not None else None, max_reorth_time,
+                                           orth_zero_tol), "Orthonormalize")
+    else:
+        _chk(W.lib.GCGE_GPU_OrthonormalizeType(W.h, start, C.byref(e), B.h if B is not None else None,
+                                               max_reorth_time, orth_zero_tol, w_orth_type.encode()),
+             "OrthonormalizeType")
     return e.value
 
 

@@ -156,6 +156,11 @@ int  GCGE_GPU_BCG(const gcge_gpu_mat *A, gcge_gpu_mv *RHS, int r_start, gcge_gpu
  * GCGE_StableMultiOrthonormalization, src/gcge_orthogonal.c:1833-1877. B may be NULL. */
 int  GCGE_GPU_Orthonormalize(gcge_gpu_mv *W, int start, int *end, const gcge_gpu_mat *B,
                              int max_reorth_time, double orth_zero_tol);
+/* The same with the variant named as the reference's w_orth_type: "multi" (the
+ * call above), "cbgs", "scbgs", or column-by-column Gram-Schmidt for any other
+ * name ("bgs", "gs"). */
+int  GCGE_GPU_OrthonormalizeType(gcge_gpu_mv *W, int start, int *end, const gcge_gpu_mat *B, int max_reorth_time,
+                                 double orth_zero_tol, const char *w_orth_type);
 
 /* ---- 4. GPU-native solver ---- */
 
@@ -185,6 +190,11 @@ typedef struct {
                                  1 Jacobi-preconditioned (z = diag(A)^-1 r, rho = r.z),
                                  the role of a user linear solver installed in
                                  ops->LinearSolver (src/gcge_xpw.c:177-191)          */
+    char   w_orth_type[8];    /* W orthonormalisation (src/gcge_eigsol.c:448-472):
+                                 "multi" (default: block projection + Cholesky-QR
+                                 twice), "cbgs" / "scbgs" (block projections, then
+                                 the eigenvectors of W^T B W, once / twice), any
+                                 other name column-by-column Gram-Schmidt          */
 } gcge_gpu_params;
 
 typedef struct {

@@ -41,6 +41,8 @@ typedef struct {
                                    1: counter-hash uniform [0,1) shared with the GPU    */
     unsigned long long seed;
     int    print_level;         /* 0 silent, 1 per-iteration line                       */
+    char   w_orth_type[8];      /* reference build only: GCGE's w_orth_type ("" = "multi";
+                                   src/gcge_eigsol.c:448-472); the restatement keeps multi */
 } gcge_oracle_params;
 
 typedef struct {

@@ -19,7 +19,7 @@ class Params(C.Structure):
         ("ev_tol", C.c_double), ("cg_rate", C.c_double), ("orth_zero_tol", C.c_double),
         ("reorth_tol", C.c_double), ("scbgs_reorth_tol", C.c_double), ("criterion_tol", C.c_double),
         ("conv_type", C.c_char * 4), ("init_rng", C.c_int), ("seed", C.c_ulonglong),
-        ("print_level", C.c_int),
+        ("print_level", C.c_int), ("w_orth_type", C.c_char * 8),
     ]
 
 
@@ -49,7 +49,7 @@ class _Lib:
         p = Params()
         self.defaults(p)
         for k, v in kw.items():
-            if k == "conv_type":
+            if k in ("conv_type", "w_orth_type"):
                 v = v.encode()
             setattr(p, k, v)
         return p

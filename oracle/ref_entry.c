@@ -53,6 +53,11 @@ int gcge_ref_solve(int n, const int *A_rp, const int *A_ci, const double *A_v,
     static char conv[4];
     strncpy(conv, p->conv_type, 3);
     s->para->conv_type = conv;
+    static char worth[8];
+    if (p->w_orth_type[0]) {
+        strncpy(worth, p->w_orth_type, 7);
+        s->para->w_orth_type = worth;
+    }
     s->para->print_para = 0;
     s->para->print_result = 0;
     int nev = p->nev;

@@ -188,8 +188,11 @@ def test_newton_reciprocal_of_inverse_iteration(ctx):
     assert np.array_equal(r[special], ref[special]) or np.allclose(r[special], ref[special], rtol=1e-15, equal_nan=True)
 
 
+@pytest.mark.parametrize("w_orth_type", [None, "cbgs", "scbgs", "bgs"])
 @pytest.mark.parametrize("use_b", [False, True])
-def test_orthonormalize(ctx, use_b):
+def test_orthonormalize(ctx, use_b, w_orth_type):
+    """B-orthonormalisation of W against B-orthonormal V, every w_orth_type variant:
+    orthonormal to 1e-12, the dependent column dropped, the inputs in the span."""
     Aa, Bb = P.fem_q1_cube(12)
     B = Bb if use_b else None
     n = Aa.n
@@ -205,7 +208,7 @@ def test_orthonormalize(ctx, use_b):
     V[:, :k0] = np.linalg.solve(L, Q.T).T
     v = ctx.multivec(n, k0 + k, V)
     dB = ctx.matrix(B) if B is not None else None
-    end = G.orthonormalize(v, k0, k0 + k, dB)
+    end = G.orthonormalize(v, k0, k0 + k, dB, w_orth_type=w_orth_type)
     assert end == k0 + k - 1                             # the dependent column was deflated
     Q = v.download()[:, :end]
     BQ = Bs @ Q if Bs is not None else Q
