@@ -120,6 +120,33 @@ extern "C" int gb_set_diag_from(gcge_gpu_ctx *ctx, double *H, int ldh, int count
     GB_LAUNCH(ctx, k_set_diag, (count + 255) / 256, 256, 0, H, ldh, count, vals);
     return GCGE_GPU_OK;
 }
+// soft locking: H[0:s, w0:m] = H[w0:m, 0:s] = 0 (the W block decoupled from the s
+// locked Ritz vectors); C[:, 0:s] = e_0 .. e_(s-1); C[0:s, s:iu] = 0
+__global__ void k_soft_lock(double *H, int ldh, int m, int w0, int s, double *C, int ldc, int iu)
+{
+    const long nh = (long)(m - w0) * s, nc = (long)m * s, nz = (long)(iu - s) * s;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nh + nc + nz; t += (long)gridDim.x * blockDim.x) {
+        if (t < nh) {
+            const int i = (int)(t % s), j = w0 + (int)(t / s);
+            H[i + (long)j * ldh] = 0.0;
+            H[j + (long)i * ldh] = 0.0;
+        } else if (t < nh + nc) {
+            const long u = t - nh;
+            const int i = (int)(u % m), j = (int)(u / m);
+            C[i + (long)j * ldc] = i == j ? 1.0 : 0.0;
+        } else {
+            const long u = t - nh - nc;
+            const int i = (int)(u % s), j = s + (int)(u / s);
+            C[i + (long)j * ldc] = 0.0;
+        }
+    }
+}
+extern "C" int gb_soft_lock(gcge_gpu_ctx *ctx, double *H, int ldh, int m, int w0, int s, double *C, int ldc, int iu)
+{
+    if (s <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_soft_lock, ctx->num_sms, 256, 0, H, ldh, m, w0, s, C, ldc, iu);
+    return GCGE_GPU_OK;
+}
 __global__ void k_sym_upper(double *H, int ldh, int m)
 {
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < (long)m * m; t += (long)gridDim.x * blockDim.x) {

@@ -189,6 +189,9 @@ int gb_set_zero(gcge_gpu_ctx *ctx, double *a, size_t count);
 int gb_copy_d(gcge_gpu_ctx *ctx, double *dst, const double *src, size_t count);
 int gb_set_diag_from(gcge_gpu_ctx *ctx, double *H, int ldh, int count, const double *vals);
 int gb_symmetrize_from_upper(gcge_gpu_ctx *ctx, double *H, int ldh, int m);
+/* soft locking of the first s Ritz vectors: H's W columns (from w0) decoupled from
+ * them, C[:, 0:s] = identity columns, C[0:s, s:iu] = 0 */
+int gb_soft_lock(gcge_gpu_ctx *ctx, double *H, int ldh, int m, int w0, int s, double *C, int ldc, int iu);
 int gb_copy_block(gcge_gpu_ctx *ctx, int rows, int cols, const double *src, int lds, double *dst, int ldd);
 /* P-coefficient assembly of ComputeP (src/gcge_xpw.c:325-330) */
 int gb_p_coef_assemble(gcge_gpu_ctx *ctx, double *coef, int ldc, int p_start, int p_ncols, int xx_nrows,

@@ -72,6 +72,7 @@ typedef struct {
     int dim_x, dim_xp, dim_xpw, last_dim_xpw, last_dim_x, unconv_bs, num_unlock, num_iter;
     double max_res, min_res, sum_res, conv_omega_norm, zero_tol;
     int orth_kind;             /* w_orth_type variant (gb_orth.h) */
+    int soft_locked;           /* Ritz pairs soft-locked in the last Rayleigh-Ritz step */
     gb_orth_ws ows;
     phase_timer tm;
 } gcg_t;
@@ -130,6 +131,8 @@ void GCGE_GPU_ParamsDefault(gcge_gpu_params *p)
     p->orth_zero_tol = 1e-16;
     strcpy(p->conv_type, "R");
     strcpy(p->w_orth_type, "multi");
+    p->opt_rr_eig_partly = 0;
+    p->multi_tol_for_lock = 1e-6;
     p->precision = 0;
     p->seed = 1;
 }
@@ -172,13 +175,36 @@ static int rr_eig(gcg_t *g)
 {
     const int ldm = g->dim_xpw;
     const int iu = g->max_dim_x < ldm ? g->max_dim_x : ldm;
-    return gb_syevx(g->ctx, ldm, g->H, ldm, 1, iu, g->eval_d, g->C, ldm, g->eig_work, g->info_d);
+    int sl = 0;
+    if (g->p.opt_rr_eig_partly && g->num_unlock > 0) {
+        /* soft locking (src/gcge_rayleighritz.c:378-394): the first unconverged
+         * index, lowered by every earlier eigenvalue within multi_tol_for_lock */
+        const int s0 = g->unlock_h[0];
+        sl = s0;
+        for (int i = s0 - 1; i >= 0; --i)
+            if (fabs(g->eval_h[i] - g->eval_h[s0]) / g->eval_h[s0] < g->p.multi_tol_for_lock) sl -= 1;
+        if (sl < 0) sl = 0;
+        if (sl > g->dim_x) sl = g->dim_x;
+        if (sl >= iu) sl = 0;
+    }
+    g->soft_locked = sl;
+    if (sl == 0) return gb_syevx(g->ctx, ldm, g->H, ldm, 1, iu, g->eval_d, g->C, ldm, g->eig_work, g->info_d);
+    /* the locked pairs keep their eigenvalues and are the unit vectors of the
+     * projected basis; only the trailing (ldm - sl) block is solved */
+    int st = gb_soft_lock(g->ctx, g->H, ldm, ldm, g->dim_xp, sl, g->C, ldm, iu);
+    if (st) return st;
+    return gb_syevx(g->ctx, ldm - sl, g->H + (size_t)sl * ldm + sl, ldm, 1, iu - sl, g->eval_d + sl,
+                    g->C + (size_t)sl * ldm + sl, ldm, g->eig_work, g->info_d);
 }
 
-/* GCGE_ComputeX (src/gcge_xpw.c:47-76): X[:, 0:nev] = V[:, 0:dim_xpw] C[:, 0:nev] */
+/* GCGE_ComputeX (src/gcge_xpw.c:47-76): X[:, s:nev] = V[:, s:dim_xpw] C[s:, s:nev], s
+ * the soft-locked count (0 without soft locking; the locked columns are unchanged) */
 static int compute_x(gcg_t *g)
 {
-    return gb_lincomb(g->ctx, g->n, g->dim_xpw, g->nev, g->V, g->ldv, g->C, g->dim_xpw, 1.0, 0.0, g->X, g->ldx, 0);
+    const int s = g->soft_locked;
+    if (s >= g->nev) return 0;
+    return gb_lincomb(g->ctx, g->n, g->dim_xpw - s, g->nev - s, g->V + s, g->ldv, g->C + (size_t)s * g->dim_xpw + s,
+                      g->dim_xpw, 1.0, 0.0, g->X + s, g->ldx, 0);
 }
 
 /* V[:, 0:nev] = X[:, 0:nev]: the pointer exchange of src/gcge_eigsol.c:312/417 as

@@ -35,7 +35,8 @@ class Params(C.Structure):
                 ("max_reorth_time", C.c_int), ("dirichlet_boundary", C.c_int), ("given_init_evec", C.c_int),
                 ("ev_tol", C.c_double), ("cg_rate", C.c_double), ("orth_zero_tol", C.c_double),
                 ("conv_type", C.c_char * 4), ("precision", C.c_int), ("seed", C.c_ulonglong),
-                ("print_level", C.c_int), ("precond", C.c_int), ("w_orth_type", C.c_char * 8)]
+                ("print_level", C.c_int), ("precond", C.c_int), ("w_orth_type", C.c_char * 8),
+                ("opt_rr_eig_partly", C.c_int), ("multi_tol_for_lock", C.c_double)]
 
 
 class Stats(C.Structure):

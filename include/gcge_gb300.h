@@ -195,6 +195,12 @@ typedef struct {
                                  twice), "cbgs" / "scbgs" (block projections, then
                                  the eigenvectors of W^T B W, once / twice), any
                                  other name column-by-column Gram-Schmidt          */
+    int    opt_rr_eig_partly; /* 1: soft locking (src/gcge_rayleighritz.c:364-400):
+                                 the converged leading Ritz pairs before the first
+                                 unconverged one (and its near-multiples) are kept,
+                                 only the trailing projected block is solved      */
+    double multi_tol_for_lock;/* 1e-6: relative gap under which an earlier
+                                 eigenvalue is taken as a multiple of it          */
 } gcge_gpu_params;
 
 typedef struct {

@@ -43,6 +43,10 @@ typedef struct {
     int    print_level;         /* 0 silent, 1 per-iteration line                       */
     char   w_orth_type[8];      /* reference build only: GCGE's w_orth_type ("" = "multi";
                                    src/gcge_eigsol.c:448-472); the restatement keeps multi */
+    char   orth_type[4];        /* reference build only: "A" orthonormalises in the A inner
+                                   product (src/gcge_eigsol.c:100-113); "" = "B" */
+    int    opt_rr_eig_partly;   /* reference build only: soft locking in the Rayleigh-Ritz
+                                   eigensolve (src/gcge_rayleighritz.c:364-400)          */
 } gcge_oracle_params;
 
 typedef struct {

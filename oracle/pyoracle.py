@@ -19,7 +19,8 @@ class Params(C.Structure):
         ("ev_tol", C.c_double), ("cg_rate", C.c_double), ("orth_zero_tol", C.c_double),
         ("reorth_tol", C.c_double), ("scbgs_reorth_tol", C.c_double), ("criterion_tol", C.c_double),
         ("conv_type", C.c_char * 4), ("init_rng", C.c_int), ("seed", C.c_ulonglong),
-        ("print_level", C.c_int), ("w_orth_type", C.c_char * 8),
+        ("print_level", C.c_int), ("w_orth_type", C.c_char * 8), ("orth_type", C.c_char * 4),
+        ("opt_rr_eig_partly", C.c_int),
     ]
 
 
@@ -49,7 +50,7 @@ class _Lib:
         p = Params()
         self.defaults(p)
         for k, v in kw.items():
-            if k in ("conv_type", "w_orth_type"):
+            if k in ("conv_type", "w_orth_type", "orth_type"):
                 v = v.encode()
             setattr(p, k, v)
         return p

@@ -53,6 +53,12 @@ int gcge_ref_solve(int n, const int *A_rp, const int *A_ci, const double *A_v,
     static char conv[4];
     strncpy(conv, p->conv_type, 3);
     s->para->conv_type = conv;
+    static char otype[4];
+    if (p->orth_type[0]) {
+        strncpy(otype, p->orth_type, 3);
+        s->para->orth_type = otype;
+    }
+    s->para->opt_rr_eig_partly = p->opt_rr_eig_partly;
     static char worth[8];
     if (p->w_orth_type[0]) {
         strncpy(worth, p->w_orth_type, 7);
