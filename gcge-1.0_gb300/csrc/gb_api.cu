@@ -705,8 +705,12 @@ static int cholqr2(gcge_gpu_ctx *ctx, int n, double *W, long ldw, int *k_io, con
             *k_io = 0;
             return GCGE_GPU_OK;
         }
-        if ((st = gb_lincomb(ctx, n, k, kept, W, ldw, ws->Tm, k, 1.0, 0.0, ws->T1, ws->ld1, kept == k))) return st;
-        if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldw))) return st;
+        if (gb_lincomb_inplace_ok(ctx, k, kept)) {
+            if ((st = gb_lincomb(ctx, n, k, kept, W, ldw, ws->Tm, k, 1.0, 0.0, W, ldw, kept == k))) return st;
+        } else {
+            if ((st = gb_lincomb(ctx, n, k, kept, W, ldw, ws->Tm, k, 1.0, 0.0, ws->T1, ws->ld1, kept == k))) return st;
+            if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldw))) return st;
+        }
         k = kept;
     }
     *k_io = k;
@@ -791,8 +795,12 @@ extern "C" int gb_orthonormalize(gcge_gpu_ctx *ctx, int n, double *V, long ldv, 
             return st;
         CUDA_TRY(ctx, cudaMemcpy2DAsync(ws->Cm + start, sizeof(double) * ldg, ws->Tm, sizeof(double) * k,
                                         sizeof(double) * k, kept, cudaMemcpyDeviceToDevice, ctx->stream));
-        if ((st = gb_lincomb(ctx, n, ldg, kept, V, ldv, ws->Cm, ldg, 1.0, 0.0, ws->T1, ws->ld1, 0))) return st;
-        if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldv))) return st;
+        if (gb_lincomb_inplace_ok(ctx, ldg, kept)) {
+            if ((st = gb_lincomb(ctx, n, ldg, kept, V, ldv, ws->Cm, ldg, 1.0, 0.0, W, ldv, 0))) return st;
+        } else {
+            if ((st = gb_lincomb(ctx, n, ldg, kept, V, ldv, ws->Cm, ldg, 1.0, 0.0, ws->T1, ws->ld1, 0))) return st;
+            if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldv))) return st;
+        }
         k = kept;
         if ((st = cholqr2(ctx, n, W, ldv, &k, B, zero_tol, ws, 1))) return st;
         *end = start + k;
@@ -864,8 +872,12 @@ static int eig_orth(gcge_gpu_ctx *ctx, int n, double *W, long ldw, int *k_io, co
         *k_io = 0;
         return GCGE_GPU_OK;
     }
-    if ((st = gb_lincomb(ctx, n, k, kept, W, ldw, ws->Cm, k, 1.0, 0.0, ws->T1, ws->ld1, 0))) return st;
-    if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldw))) return st;
+    if (gb_lincomb_inplace_ok(ctx, k, kept)) {
+        if ((st = gb_lincomb(ctx, n, k, kept, W, ldw, ws->Cm, k, 1.0, 0.0, W, ldw, 0))) return st;
+    } else {
+        if ((st = gb_lincomb(ctx, n, k, kept, W, ldw, ws->Cm, k, 1.0, 0.0, ws->T1, ws->ld1, 0))) return st;
+        if ((st = gb_axpby(ctx, n, kept, 1.0, ws->T1, ws->ld1, 0.0, W, ldw))) return st;
+    }
     *k_io = kept;
     return GCGE_GPU_OK;
 }

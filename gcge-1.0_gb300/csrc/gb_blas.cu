@@ -1073,6 +1073,11 @@ k_lincomb(int n, int k1, int k2, const double *__restrict__ X, long ldx, const d
     }
 }
 
+extern "C" int gb_lincomb_inplace_ok(const gcge_gpu_ctx *ctx, int k1, int k2)
+{
+    return ctx->tc && gb_lincomb_tc_inplace_ok(k1, k2);
+}
+
 extern "C" int gb_lincomb(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *X, long ldx,
                           const double *C_dev, int ldc, double alpha, double beta, double *Y, long ldy,
                           int upper)

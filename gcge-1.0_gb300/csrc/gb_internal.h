@@ -104,6 +104,9 @@ int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *V, long l
 /* FP64-accurate Y = alpha X C + beta Y on the tensor cores (gb_ozaki.cu), for k1 where
  * gb_lincomb_tc_ok(k1) holds */
 int gb_lincomb_tc_ok(int k1);
+int gb_lincomb_tc_inplace_ok(int k1, int k2);
+/* 1 when gb_lincomb may write Y over columns of X (same rows, same ld) */
+int gb_lincomb_inplace_ok(const gcge_gpu_ctx *ctx, int k1, int k2);
 int gb_lincomb_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double *X, long ldx, const double *C, int ldc,
                   double alpha, double beta, double *Y, long ldy, int upper);
 

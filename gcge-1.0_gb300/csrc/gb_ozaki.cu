@@ -788,6 +788,11 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
 }
 
 extern "C" int gb_lincomb_tc_ok(int k1) { return k1 <= LC_MAX_K; }
+// Y may overlap X's columns (the same rows, the same leading dimension) when one
+// column tile covers the output: a CTA reads every entry of its row tile before
+// its drain writes that tile's rows, and walks only its own tiles (the
+// next-tile prefetch and scale pass included)
+extern "C" int gb_lincomb_tc_inplace_ok(int k1, int k2) { return k1 <= LC_MAX_K && k2 <= TC_N; }
 
 // Y = alpha X C + beta Y (C: k1 x k2 column-major on the device, upper: only
 // i <= j of C is used) to FP64 accuracy on the tensor cores.

@@ -381,9 +381,15 @@ static int compute_p(gcg_t *g)
     ph_end(g);
     ph_begin(g, PH_P_AXPY);
     const int p_end_tmp = p_end - g->nev;
-    TRY(gb_lincomb(ctx, g->n, ldc, p_end_tmp, g->V, g->ldv, g->C + (size_t)g->nev * ldc, ldc, 1.0, 0.0, g->S1,
-                   g->lds, 0));
-    TRY(gb_axpby(ctx, g->n, p_end_tmp, 1.0, g->S1, g->lds, 0.0, g->V + g->nev, g->ldv));
+    if (gb_lincomb_inplace_ok(ctx, ldc, p_end_tmp)) {
+        /* P = V C_P written over V[:, nev:] directly (one column tile) */
+        TRY(gb_lincomb(ctx, g->n, ldc, p_end_tmp, g->V, g->ldv, g->C + (size_t)g->nev * ldc, ldc, 1.0, 0.0,
+                       g->V + g->nev, g->ldv, 0));
+    } else {
+        TRY(gb_lincomb(ctx, g->n, ldc, p_end_tmp, g->V, g->ldv, g->C + (size_t)g->nev * ldc, ldc, 1.0, 0.0, g->S1,
+                       g->lds, 0));
+        TRY(gb_axpby(ctx, g->n, p_end_tmp, 1.0, g->S1, g->lds, 0.0, g->V + g->nev, g->ldv));
+    }
     ph_end(g);
     g->dim_xp = p_end;
     return 0;
