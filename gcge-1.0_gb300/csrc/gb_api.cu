@@ -298,53 +298,84 @@ __global__ void k_d2f_vals(long n, const double *a, float *b)
         b[t] = (float)a[t];
 }
 
+// structural check of an uploaded CSR matrix: res[0] = 1 if a row pointer
+// decreases or a column lies outside [0, n); res[1] = the longest row
+__global__ void k_csr_check(int n, int nnz, const int *__restrict__ rp, const int *__restrict__ ci, int *res)
+{
+    int bad = 0, mr = 0;
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int len = rp[i + 1] - rp[i];
+        bad |= len < 0;
+        mr = max(mr, len);
+    }
+    for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += stride) {
+        const int c = ci[e];
+        bad |= c < 0 || c >= n;
+    }
+    for (int o = 16; o; o >>= 1) {
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+        mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (bad) atomicOr(res, 1);
+        atomicMax(res + 1, mr);
+    }
+}
+
+// The structure is checked on the device after the upload (a host loop over
+// the column indices cost ~20 ms per 40 M entries, on the path of every
+// host-buffer solve); the result is read back with the creation's final sync.
 extern "C" int GCGE_GPU_MatCreate(gcge_gpu_ctx *ctx, int n, const int *rowptr, const int *col, const double *val,
                                   int keep_fp32, gcge_gpu_mat **out)
 {
     if (!ctx || !out || n <= 0 || !rowptr || (!col && rowptr[n] > 0) || (!val && rowptr[n] > 0))
         return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     *out = nullptr;
-    // host-side structural checks: monotone row pointers, columns in range
-    if (rowptr[0] != 0) return gb_fail(ctx, GCGE_GPU_ERR_CSR);
-    int maxrow = 0;
-    for (int i = 0; i < n; ++i) {
-        if (rowptr[i + 1] < rowptr[i]) return gb_fail(ctx, GCGE_GPU_ERR_CSR);
-        if (rowptr[i + 1] - rowptr[i] > maxrow) maxrow = rowptr[i + 1] - rowptr[i];
-    }
+    if (rowptr[0] != 0 || rowptr[n] < 0) return gb_fail(ctx, GCGE_GPU_ERR_CSR);
     const int nnz = rowptr[n];
-    for (int e = 0; e < nnz; ++e)
-        if (col[e] < 0 || col[e] >= n) return gb_fail(ctx, GCGE_GPU_ERR_CSR);
     gcge_gpu_mat *A = (gcge_gpu_mat *)calloc(1, sizeof(gcge_gpu_mat));
     if (!A) return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
     A->ctx = ctx;
     A->n = n;
     A->nnz = nnz;
-    A->max_row_nnz = maxrow;
     size_t nz = nnz > 0 ? (size_t)nnz : 1;
+    int *chk = nullptr;
     if (cudaMalloc(&A->rp, sizeof(int) * (n + 1)) != cudaSuccess || cudaMalloc(&A->ci, sizeof(int) * nz) != cudaSuccess ||
         cudaMalloc(&A->v, sizeof(double) * nz) != cudaSuccess ||
-        (keep_fp32 && cudaMalloc(&A->v32, sizeof(float) * nz) != cudaSuccess)) {
+        (keep_fp32 && cudaMalloc(&A->v32, sizeof(float) * nz) != cudaSuccess) ||
+        cudaMalloc(&chk, 2 * sizeof(int)) != cudaSuccess) {
+        if (chk) cudaFree(chk);
         GCGE_GPU_MatDestroy(A);
         return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
     }
-    if (cudaMemcpyAsync(A->rp, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+    int h[2] = {0, 0};
+    if (cudaMemsetAsync(chk, 0, 2 * sizeof(int), ctx->stream) != cudaSuccess ||
+        cudaMemcpyAsync(A->rp, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
         (nnz && cudaMemcpyAsync(A->ci, col, sizeof(int) * nnz, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) ||
         (nnz && cudaMemcpyAsync(A->v, val, sizeof(double) * nnz, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)) {
+        cudaFree(chk);
         GCGE_GPU_MatDestroy(A);
         return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
     }
+    k_csr_check<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(n, nnz, A->rp, A->ci, chk);
+    ctx->launches++;
     if (keep_fp32 && nnz) {
         k_d2f_vals<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(nnz, A->v, A->v32);
         ctx->launches++;
-        if (gb_check_launch(ctx)) {
-            GCGE_GPU_MatDestroy(A);
-            return GCGE_GPU_ERR_CUDA;
-        }
     }
-    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    if (gb_check_launch(ctx) || cudaMemcpyAsync(h, chk, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        cudaFree(chk);
         GCGE_GPU_MatDestroy(A);
         return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
     }
+    cudaFree(chk);
+    if (h[0]) {
+        GCGE_GPU_MatDestroy(A);
+        return gb_fail(ctx, GCGE_GPU_ERR_CSR);
+    }
+    A->max_row_nnz = h[1];
     *out = A;
     return GCGE_GPU_OK;
 }

@@ -231,6 +231,13 @@ def test_matrix_csr_validation(ctx):
     bad2.rowptr[4] = bad2.rowptr[5] + 1
     with pytest.raises(G.GcgeGpuError):
         ctx.matrix(bad2)
+    bad3 = P.CSR(A.rowptr.copy(), A.col.copy(), A.val.copy())
+    bad3.col[-1] = -1                                   # checked on the device after the upload
+    with pytest.raises(G.GcgeGpuError) as e:
+        ctx.matrix(bad3)
+    assert e.value.status == 4
+    dA = ctx.matrix(A)                                  # a valid matrix after the rejected ones
+    assert dA.n == A.n
 
 
 def test_range_checks(ctx):
