@@ -160,9 +160,10 @@ static int rr_matrix(gcg_t *g)
     /* VTAW (src/gcge_rayleighritz.c:35-81): AW = A W into S1 */
     const int w_len = ldm - dim_xp, xp_len = dim_xp;
     TRY(gb_spmm(ctx, g->A, g->V + dim_xp, g->ldv, g->S1, g->lds, w_len, 1.0, NULL, 0.0, NULL));
-    if (xp_len > 0)
-        TRY(gb_gram(ctx, n, xp_len, w_len, g->V, g->ldv, g->S1, g->lds, g->H + (size_t)dim_xp * ldm, ldm, 0));
-    TRY(gb_gram(ctx, n, w_len, w_len, g->V + dim_xp, g->ldv, g->S1, g->lds, g->H + (size_t)dim_xp * ldm + dim_xp, ldm, 1));
+    /* [X P W]^T (A W) in one Gram: H[0:ldm, dim_xp:ldm] (the W^T A W block in full;
+     * its lower half is then replaced by the mirrored upper half) */
+    (void)xp_len;
+    TRY(gb_gram(ctx, n, ldm, w_len, g->V, g->ldv, g->S1, g->lds, g->H + (size_t)dim_xp * ldm, ldm, 0));
     TRY(gb_symmetrize_from_upper(ctx, g->H, ldm, ldm));
     return 0;
 fail:
