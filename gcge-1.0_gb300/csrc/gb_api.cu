@@ -662,7 +662,13 @@ extern "C" int GCGE_GPU_BCG(const gcge_gpu_mat *A, gcge_gpu_mv *RHS, int r_start
     size_t bytes = gb_bcg_work_bytes(A->n, k, precision);
     void *work = nullptr;
     CUDA_TRY(ctx, cudaMalloc(&work, bytes));
-    gb_bcg_args args = {A->n, k, cg_max_it, precision, cg_rate};
+    gb_bcg_args args;
+    memset(&args, 0, sizeof(args));
+    args.n = A->n;
+    args.k = k;
+    args.max_it = cg_max_it;
+    args.precision = precision;
+    args.rate = cg_rate;
     int st = gb_bcg(ctx, A, RHS->d + r_start, RHS->ld, W->d + w_start, W->ld, &args, work, bytes);
     cudaStreamSynchronize(ctx->stream);
     cudaFree(work);

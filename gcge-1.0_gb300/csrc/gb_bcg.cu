@@ -668,7 +668,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     if ((st = k <= 128 ? bcg_rounds32(ctx, A, R, D, P, W, ld, a, &s) : bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s)))
         return st;
     GB_LAUNCH(ctx, k_add_f2d, row_grid(ctx, n), 256, 0, n, k, D, ld, X, ldx);
-    return gb_convert_f2d(ctx, n, k, R, ld, RHS, ldr);
+    return a->residual_unused ? GCGE_GPU_OK : gb_convert_f2d(ctx, n, k, R, ld, RHS, ldr);
 }
 
 __global__ void k_axpy32(int n, int k, float a, const float *__restrict__ X, float *__restrict__ Y, long ld)

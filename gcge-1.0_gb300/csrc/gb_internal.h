@@ -161,6 +161,8 @@ typedef struct {
     int rhs_is_residual;       /* RHS already holds RHS - A X: skip the initial product */
     const double *dinv;        /* Jacobi preconditioner 1/diag(A) (FP64 rounds) or NULL: plain CG */
     const float *dinv32;       /* the same for the FP32 rounds */
+    int residual_unused;       /* the caller does not read RHS afterwards: the mixed
+                                  form skips writing the final residual back into it */
 } gb_bcg_args;
 /* 1 / diag(A) in FP64 and FP32, computed once per matrix values (a zero or missing
  * diagonal entry gives 1) */

@@ -222,9 +222,21 @@ static int check_conv(gcg_t *g)
     const int nu = g->num_unlock, n = g->n;
     if (nu > 0) {
         CTRY(cudaMemcpyAsync(g->unlock_d, g->unlock_h, sizeof(int) * nu, cudaMemcpyHostToDevice, ctx->stream));
-        TRY(gb_gather_cols(ctx, n, nu, g->X, g->ldx, g->unlock_d, g->S1, g->lds, NULL, 0));
-        TRY(gb_spmm_ab(ctx, g->A, g->B, g->S1, g->lds, g->S2, g->S3, g->lds, nu));
-        TRY(gb_residual_norms(ctx, n, nu, g->S1, g->lds, g->S2, g->lds, g->B ? g->S3 : NULL, g->lds, g->eval_d,
+        /* the unlocked columns are usually a contiguous range of X (the trailing
+         * unconverged pairs): then the products read X in place, else a gather */
+        int contiguous = 1;
+        for (int j = 1; j < nu; ++j)
+            if (g->unlock_h[j] != g->unlock_h[0] + j) contiguous = 0;
+        const double *Xu = g->S1;
+        long ldu = g->lds;
+        if (contiguous) {
+            Xu = g->X + g->unlock_h[0];
+            ldu = g->ldx;
+        } else {
+            TRY(gb_gather_cols(ctx, n, nu, g->X, g->ldx, g->unlock_d, g->S1, g->lds, NULL, 0));
+        }
+        TRY(gb_spmm_ab(ctx, g->A, g->B, Xu, ldu, g->S2, g->S3, g->lds, nu));
+        TRY(gb_residual_norms(ctx, n, nu, Xu, ldu, g->S2, g->lds, g->B ? g->S3 : NULL, g->lds, g->eval_d,
                               g->unlock_d, g->res_d, strcmp(g->p.conv_type, "BR") == 0));
         CTRY(cudaMemcpyAsync(g->res_h, g->res_d, sizeof(double) * 3 * nu, cudaMemcpyDeviceToHost, ctx->stream));
     }
@@ -307,6 +319,7 @@ static int compute_w(gcg_t *g)
     a.rhs_is_residual = 0;
     a.dinv = NULL;
     a.dinv32 = NULL;
+    a.residual_unused = 1;     /* S1 is scratch after the W step */
     if (g->p.precond == 1) {
         /* Jacobi: the diagonal inverse is cached on the matrix (recomputed after new values) */
         TRY(gb_mat_dinv(ctx, (gcge_gpu_mat *)g->A));
