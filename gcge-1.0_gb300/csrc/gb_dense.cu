@@ -388,6 +388,118 @@ k_tridiag(int m, const double *__restrict__ H, int ldh, double *__restrict__ Aw,
     }
 }
 
+// The same reduction with the lower triangle packed in shared memory (column c,
+// rows c..m-1, at c m - c (c - 1) / 2), for m <= TD_SMEM_MAX_M: the row-wise half
+// of the matrix-vector product then reads shared memory instead of global rows
+// at a stride of m doubles, and the rank-2 update stays on chip. Same operations
+// in the same order as k_tridiag; the reflectors are written back to Aw (columns
+// i, rows i+1..) at the end for the back-transformation.
+#define TD_SMEM_MAX_M 230
+static size_t td_smem_bytes(int m) { return sizeof(double) * ((size_t)m * (m + 1) / 2 + 2 * (size_t)m); }
+
+__global__ void __launch_bounds__(1024)
+k_tridiag_smem(int m, const double *__restrict__ H, int ldh, double *__restrict__ Aw, double *__restrict__ d,
+               double *__restrict__ e, double *__restrict__ tau)
+{
+    extern __shared__ double sm[];
+    double *L = sm;                                   // packed lower triangle
+    double *v = sm + (size_t)m * (m + 1) / 2;         // m
+    double *w = v + m;                                // m
+    __shared__ double red[32];
+    __shared__ double s_alpha, s_beta, s_tau, s_K;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    auto off = [m](int c) { return (long)c * m - (long)c * (c - 1) / 2; };
+    for (int c = wid; c < m; c += nw)
+        for (int r = c + lane; r < m; r += 32) L[off(c) + (r - c)] = H[r + (long)c * ldh];
+    __syncthreads();
+    for (int i = 0; i + 2 < m; ++i) {
+        const int len = m - i - 1;
+        double *col = L + off(i) + 1;                 // x = A[i+1:m, i]
+        double s = 0;
+        for (int r = 1 + tid; r < len; r += nt) s = fma(col[r], col[r], s);
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+        if (lane == 0) red[wid] = s;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0;
+            for (int q = 0; q < nw; ++q) t += red[q];
+            const double alpha = col[0];
+            if (t == 0.0) {
+                s_tau = 0.0;
+                s_beta = alpha;
+            } else {
+                const double beta = -copysign(sqrt(alpha * alpha + t), alpha);
+                s_tau = (beta - alpha) / beta;
+                s_beta = beta;
+                s_alpha = 1.0 / (alpha - beta);
+            }
+            d[i] = L[off(i)];
+            e[i] = s_beta;
+            tau[i] = s_tau;
+        }
+        __syncthreads();
+        const double tv = s_tau;
+        if (tv == 0.0) {
+            for (int r = 1 + tid; r < len; r += nt) col[r] = 0.0;
+            __syncthreads();
+            continue;
+        }
+        const double sc = s_alpha;
+        for (int r = tid; r < len; r += nt) {
+            const double vr = (r == 0) ? 1.0 : col[r] * sc;
+            v[r] = vr;
+            if (r > 0) col[r] = vr;
+        }
+        __syncthreads();
+        // p = tau * A22 v, A22 = A[i+1:, i+1:]: warp per row r, A22[r, c] from
+        // column c (c <= r) or column r (c > r) of the packed triangle
+        const int b = i + 1;
+        for (int r = wid; r < len; r += nw) {
+            double a0 = 0;
+            for (int c = lane; c < len; c += 32) {
+                const double a = (c <= r) ? L[off(b + c) + (r - c)] : L[off(b + r) + (c - r)];
+                a0 = fma(a, v[c], a0);
+            }
+            for (int o = 16; o; o >>= 1) a0 += __shfl_xor_sync(FULL, a0, o);
+            if (lane == 0) w[r] = tv * a0;
+        }
+        __syncthreads();
+        s = 0;
+        for (int r = tid; r < len; r += nt) s = fma(w[r], v[r], s);
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+        if (lane == 0) red[wid] = s;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0;
+            for (int q = 0; q < nw; ++q) t += red[q];
+            s_K = 0.5 * tv * t;
+        }
+        __syncthreads();
+        const double K = s_K;
+        for (int r = tid; r < len; r += nt) w[r] = w[r] - K * v[r];
+        __syncthreads();
+        for (int c = wid; c < len; c += nw) {
+            const double vc = v[c], wc = w[c];
+            double *Lc = L + off(b + c);
+            for (int r = c + lane; r < len; r += 32) Lc[r - c] -= v[r] * wc + w[r] * vc;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (m >= 2) {
+            d[m - 2] = L[off(m - 2)];
+            e[m - 2] = L[off(m - 2) + 1];
+            tau[m - 2] = 0.0;
+        }
+        d[m - 1] = L[off(m - 1)];
+        e[m - 1] = 0.0;
+        tau[m - 1] = 0.0;
+    }
+    // reflectors (and the rest of the lower triangle) back to Aw for the back-transformation
+    for (int c = wid; c < m; c += nw)
+        for (int r = c + lane; r < m; r += 32) Aw[r + (long)c * m] = L[off(c) + (r - c)];
+}
+
 // ---------------------------------------------------------------- cluster tridiagonalisation
 // The same reduction as k_tridiag (dsytd2 "L": reflectors in the columns of Aw,
 // d, e, tau) spread over a thread-block cluster of TC CTAs, so that the FP64 work
@@ -1005,7 +1117,17 @@ extern "C" int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int 
         int st = td_cluster_launch(ctx, tc, m, H, ldh, Aw, d, e, tau);
         if (st) return st;
     } else {
-        GB_LAUNCH(ctx, k_tridiag, 1, tthreads, 2 * m * sizeof(double), m, H, ldh, Aw, d, e, tau);
+        static bool td_attr = false;
+        if (!td_attr) {
+            if (cudaFuncSetAttribute(k_tridiag_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)td_smem_bytes(TD_SMEM_MAX_M)) != cudaSuccess)
+                return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+            td_attr = true;
+        }
+        if (m <= TD_SMEM_MAX_M)
+            GB_LAUNCH(ctx, k_tridiag_smem, 1, tthreads, td_smem_bytes(m), m, H, ldh, Aw, d, e, tau);
+        else
+            GB_LAUNCH(ctx, k_tridiag, 1, tthreads, 2 * m * sizeof(double), m, H, ldh, Aw, d, e, tau);
     }
     const int warps_per_block = 1;     // one eigenvalue per SM: the Sturm chains use the FP64 pipe
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
