@@ -156,10 +156,74 @@ extern "C" int GCGE_GPU_Init(int device, gcge_gpu_ctx **out)
     return GCGE_GPU_OK;
 }
 
+// ---------------------------------------------------------------- device block cache
+// The workspace of a solve (the basis V, scratch blocks, the orthonormalisation
+// and block-CG work; several GB at n ~ 1e6) goes back to the context instead of
+// cudaFree, so repeated solves on a context reuse it rather than paying
+// cudaMalloc/cudaFree of every block each time. Blocks are used on the context's
+// stream only, so handing one to a later request is stream-ordered.
+extern "C" int gb_dev_alloc(gcge_gpu_ctx *ctx, void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (bytes == 0) bytes = 8;
+    int best = -1;
+    for (int i = 0; i < ctx->nblk; ++i) {
+        const gb_block &b = ctx->blk[i];
+        if (!b.used && b.bytes >= bytes && b.bytes <= 2 * bytes && (best < 0 || b.bytes < ctx->blk[best].bytes))
+            best = i;
+    }
+    if (best >= 0) {
+        ctx->blk[best].used = 1;
+        *p = ctx->blk[best].p;
+        return GCGE_GPU_OK;
+    }
+    void *q = nullptr;
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        // give the unused cached blocks back and try once more
+        int k = 0;
+        for (int i = 0; i < ctx->nblk; ++i) {
+            if (ctx->blk[i].used) ctx->blk[k++] = ctx->blk[i];
+            else cudaFree(ctx->blk[i].p);
+        }
+        ctx->nblk = k;
+        if (cudaMalloc(&q, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return GCGE_GPU_ERR_NOMEM;
+        }
+    }
+    if (ctx->nblk == ctx->blk_cap) {
+        const int nc = ctx->blk_cap ? 2 * ctx->blk_cap : 64;
+        gb_block *nb = (gb_block *)realloc(ctx->blk, sizeof(gb_block) * nc);
+        if (!nb) {
+            cudaFree(q);
+            return GCGE_GPU_ERR_NOMEM;
+        }
+        ctx->blk = nb;
+        ctx->blk_cap = nc;
+    }
+    ctx->blk[ctx->nblk++] = gb_block{q, bytes, 1};
+    *p = q;
+    return GCGE_GPU_OK;
+}
+
+extern "C" void gb_dev_free(gcge_gpu_ctx *ctx, void *p)
+{
+    if (!p) return;
+    for (int i = 0; i < ctx->nblk; ++i)
+        if (ctx->blk[i].p == p) {
+            ctx->blk[i].used = 0;
+            return;
+        }
+    cudaFree(p);
+}
+
 extern "C" int GCGE_GPU_Finalize(gcge_gpu_ctx *ctx)
 {
     if (!ctx) return GCGE_GPU_OK;
     cudaStreamSynchronize(ctx->stream);
+    for (int i = 0; i < ctx->nblk; ++i) cudaFree(ctx->blk[i].p);
+    free(ctx->blk);
     if (ctx->prof_ev) {
         for (int i = 0; i < 2 * GB_PROF_SLOTS; ++i)
             if (ctx->prof_ev[i]) cudaEventDestroy(ctx->prof_ev[i]);
@@ -679,6 +743,7 @@ extern "C" int GCGE_GPU_BCG(const gcge_gpu_mat *A, gcge_gpu_mv *RHS, int r_start
 extern "C" int gb_orth_ws_alloc(gcge_gpu_ctx *ctx, gb_orth_ws *ws, int n, int max_width, int max_start)
 {
     memset(ws, 0, sizeof(*ws));
+    ws->ctx = ctx;
     ws->max_width = max_width;
     ws->max_start = max_start;
     ws->ld1 = (max_width + 1) & ~1;
@@ -686,16 +751,16 @@ extern "C" int gb_orth_ws_alloc(gcge_gpu_ctx *ctx, gb_orth_ws *ws, int n, int ma
     // Gram blocks up to [V W]^T (B W): (max_start + max_width) x max_width
     size_t sk = ((size_t)(max_start > 0 ? max_start : 1) + max_width) * max_width;
     ws->g_cap = kk > sk ? kk : sk;
-    if (cudaMalloc(&ws->T1, sizeof(double) * (size_t)n * ws->ld1) != cudaSuccess ||
-        cudaMalloc(&ws->G, sizeof(double) * (kk > sk ? kk : sk)) != cudaSuccess ||
-        cudaMalloc(&ws->Tm, sizeof(double) * kk) != cudaSuccess ||
-        cudaMalloc(&ws->Cm, sizeof(double) * ((size_t)max_start + max_width) * max_width) != cudaSuccess ||
-        cudaMalloc(&ws->chol_work, sizeof(double) * 2 * kk) != cudaSuccess ||
-        cudaMalloc(&ws->small, sizeof(double) * 64) != cudaSuccess ||
-        cudaMalloc(&ws->kept_dev, sizeof(int) * 4) != cudaSuccess ||
-        cudaMalloc(&ws->ev_work, sizeof(double) * gb_syevx_work_doubles(max_width)) != cudaSuccess ||
-        cudaMalloc(&ws->ev_val, sizeof(double) * max_width) != cudaSuccess ||
-        cudaMalloc(&ws->ev_info, sizeof(int) * 4) != cudaSuccess) {
+    if (gb_dev_alloc(ctx, (void **)&ws->T1, sizeof(double) * (size_t)n * ws->ld1) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->G, sizeof(double) * (kk > sk ? kk : sk)) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->Tm, sizeof(double) * kk) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->Cm, sizeof(double) * ((size_t)max_start + max_width) * max_width) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->chol_work, sizeof(double) * 2 * kk) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->small, sizeof(double) * 64) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->kept_dev, sizeof(int) * 4) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->ev_work, sizeof(double) * gb_syevx_work_doubles(max_width)) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->ev_val, sizeof(double) * max_width) != GCGE_GPU_OK ||
+        gb_dev_alloc(ctx, (void **)&ws->ev_info, sizeof(int) * 4) != GCGE_GPU_OK) {
         gb_orth_ws_free(ws);
         return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
     }
@@ -704,16 +769,16 @@ extern "C" int gb_orth_ws_alloc(gcge_gpu_ctx *ctx, gb_orth_ws *ws, int n, int ma
 
 extern "C" void gb_orth_ws_free(gb_orth_ws *ws)
 {
-    if (ws->T1) cudaFree(ws->T1);
-    if (ws->G) cudaFree(ws->G);
-    if (ws->Tm) cudaFree(ws->Tm);
-    if (ws->Cm) cudaFree(ws->Cm);
-    if (ws->chol_work) cudaFree(ws->chol_work);
-    if (ws->small) cudaFree(ws->small);
-    if (ws->kept_dev) cudaFree(ws->kept_dev);
-    if (ws->ev_work) cudaFree(ws->ev_work);
-    if (ws->ev_val) cudaFree(ws->ev_val);
-    if (ws->ev_info) cudaFree(ws->ev_info);
+    gb_dev_free(ws->ctx, ws->T1);
+    gb_dev_free(ws->ctx, ws->G);
+    gb_dev_free(ws->ctx, ws->Tm);
+    gb_dev_free(ws->ctx, ws->Cm);
+    gb_dev_free(ws->ctx, ws->chol_work);
+    gb_dev_free(ws->ctx, ws->small);
+    gb_dev_free(ws->ctx, ws->kept_dev);
+    gb_dev_free(ws->ctx, ws->ev_work);
+    gb_dev_free(ws->ctx, ws->ev_val);
+    gb_dev_free(ws->ctx, ws->ev_info);
     memset(ws, 0, sizeof(*ws));
 }
 

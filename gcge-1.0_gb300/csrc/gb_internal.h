@@ -25,6 +25,13 @@ extern "C" {
 enum { GB_K_SPMM64, GB_K_SPMM32, GB_K_GRAM, GB_K_LINCOMB, GB_K_BCGVEC, GB_K_BLAS1, GB_K_DENSE, GB_K_EIG,
        GB_K_REDUCE, GB_K_SPMMPAIR, GB_PROF_CLASSES };
 
+/* a device block held by the context's cache (gb_dev_alloc / gb_dev_free) */
+typedef struct {
+    void *p;
+    size_t bytes;
+    int used;
+} gb_block;
+
 struct gcge_gpu_ctx {
     int device;
     int num_sms;
@@ -62,6 +69,8 @@ struct gcge_gpu_ctx {
     size_t pairbuf_cap;        /* floats */
     int *dev_pairflag;         /* device word: epoch of the last split that met |x| >= 2^100 */
     int pair_epoch;
+    gb_block *blk;             /* workspace blocks kept for later solves on this context */
+    int nblk, blk_cap;
 };
 
 struct gcge_gpu_mat {
@@ -83,6 +92,12 @@ struct gcge_gpu_mv {
     long ld;
     double *d;
 };
+
+/* device workspace through the context's block cache: a released block is kept
+ * and handed to a later request of between its size and half of it (best fit);
+ * all are freed by GCGE_GPU_Finalize (and unused ones when cudaMalloc fails) */
+int  gb_dev_alloc(gcge_gpu_ctx *ctx, void **p, size_t bytes);
+void gb_dev_free(gcge_gpu_ctx *ctx, void *p);
 
 /* profiling hooks around a launch: class, algorithmic bytes and flops */
 void gb_prof_begin(gcge_gpu_ctx *ctx, int cls, double bytes, double flops);

@@ -12,6 +12,7 @@ extern "C" {
 #endif
 
 typedef struct {
+    gcge_gpu_ctx *ctx;         /* owner of the blocks (its block cache) */
     int max_width, max_start;
     size_t g_cap;    /* doubles in G */
     double *T1;      /* n x ld1 block: B*W and the re-combined columns */

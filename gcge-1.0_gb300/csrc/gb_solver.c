@@ -428,7 +428,7 @@ static void gcg_free(gcg_t *g)
                    g->chol_work, g->eval_d, g->eig_work, g->res_d, g->lam_d, g->dsmall, g->unlock_d, g->kept_d,
                    g->info_d, g->pos_d};
     for (size_t i = 0; i < sizeof(dev) / sizeof(dev[0]); ++i)
-        if (dev[i]) cudaFree(dev[i]);
+        if (dev[i]) gb_dev_free(g->ctx, dev[i]);
     gb_orth_ws_free(&g->ows);
     free(g->eval_h);
     free(g->res_h);
@@ -439,7 +439,7 @@ static void gcg_free(gcg_t *g)
         if (g->tm.ev[i]) cudaEventDestroy(g->tm.ev[i]);
 }
 
-static int dmalloc(void **p, size_t bytes) { return cudaMalloc(p, bytes > 0 ? bytes : 8) == cudaSuccess ? 0 : 1; }
+static int dmalloc(gcge_gpu_ctx *ctx, void **p, size_t bytes) { return gb_dev_alloc(ctx, p, bytes) ? 1 : 0; }
 
 static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat *B, const gcge_gpu_params *pin,
                       double *eval, gcge_gpu_mv *evec, gcge_gpu_stats *stats);
@@ -499,22 +499,22 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
     const size_t vs = g->V_size, vs2 = vs * vs;
     for (int i = 0; i < 128; ++i)
         if (cudaEventCreate(&g->tm.ev[i]) != cudaSuccess) { st = gb_fail(ctx, GCGE_GPU_ERR_CUDA); goto fail; }
-    if (dmalloc((void **)&g->V, sizeof(double) * (size_t)n * g->ldv) || dmalloc((void **)&g->S1, sizeof(double) * (size_t)n * g->lds) ||
-        dmalloc((void **)&g->S2, sizeof(double) * (size_t)n * g->lds) || dmalloc((void **)&g->S3, sizeof(double) * (size_t)n * g->lds) ||
-        dmalloc((void **)&g->H, sizeof(double) * vs2) || dmalloc((void **)&g->C, sizeof(double) * vs2) ||
-        dmalloc((void **)&g->Ctmp, sizeof(double) * vs2) || dmalloc((void **)&g->AApp, sizeof(double) * vs2) ||
-        dmalloc((void **)&g->Gs, sizeof(double) * vs2) || dmalloc((void **)&g->Ts, sizeof(double) * vs2) ||
-        dmalloc((void **)&g->chol_work, sizeof(double) * 2 * vs2) || dmalloc((void **)&g->eval_d, sizeof(double) * vs) ||
-        dmalloc((void **)&g->eig_work, sizeof(double) * gb_syevx_work_doubles((int)vs)) ||
-        dmalloc((void **)&g->res_d, sizeof(double) * 3 * (nev + 8)) || dmalloc((void **)&g->lam_d, sizeof(double) * (vs + 8)) ||
-        dmalloc((void **)&g->dsmall, sizeof(double) * 64) || dmalloc((void **)&g->unlock_d, sizeof(int) * vs) ||
-        dmalloc((void **)&g->kept_d, sizeof(int) * 4) || dmalloc((void **)&g->info_d, sizeof(int) * 4) ||
-        dmalloc((void **)&g->pos_d, sizeof(int) * vs)) {
+    if (dmalloc(ctx, (void **)&g->V, sizeof(double) * (size_t)n * g->ldv) || dmalloc(ctx, (void **)&g->S1, sizeof(double) * (size_t)n * g->lds) ||
+        dmalloc(ctx, (void **)&g->S2, sizeof(double) * (size_t)n * g->lds) || dmalloc(ctx, (void **)&g->S3, sizeof(double) * (size_t)n * g->lds) ||
+        dmalloc(ctx, (void **)&g->H, sizeof(double) * vs2) || dmalloc(ctx, (void **)&g->C, sizeof(double) * vs2) ||
+        dmalloc(ctx, (void **)&g->Ctmp, sizeof(double) * vs2) || dmalloc(ctx, (void **)&g->AApp, sizeof(double) * vs2) ||
+        dmalloc(ctx, (void **)&g->Gs, sizeof(double) * vs2) || dmalloc(ctx, (void **)&g->Ts, sizeof(double) * vs2) ||
+        dmalloc(ctx, (void **)&g->chol_work, sizeof(double) * 2 * vs2) || dmalloc(ctx, (void **)&g->eval_d, sizeof(double) * vs) ||
+        dmalloc(ctx, (void **)&g->eig_work, sizeof(double) * gb_syevx_work_doubles((int)vs)) ||
+        dmalloc(ctx, (void **)&g->res_d, sizeof(double) * 3 * (nev + 8)) || dmalloc(ctx, (void **)&g->lam_d, sizeof(double) * (vs + 8)) ||
+        dmalloc(ctx, (void **)&g->dsmall, sizeof(double) * 64) || dmalloc(ctx, (void **)&g->unlock_d, sizeof(int) * vs) ||
+        dmalloc(ctx, (void **)&g->kept_d, sizeof(int) * 4) || dmalloc(ctx, (void **)&g->info_d, sizeof(int) * 4) ||
+        dmalloc(ctx, (void **)&g->pos_d, sizeof(int) * vs)) {
         st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
         goto fail;
     }
     g->bcg_bytes = gb_bcg_work_bytes(n, g->bs, pin->precision);
-    if (dmalloc(&g->bcg_work, g->bcg_bytes)) { st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM); goto fail; }
+    if (dmalloc(ctx, &g->bcg_work, g->bcg_bytes)) { st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM); goto fail; }
     TRY(gb_orth_ws_alloc(ctx, &g->ows, n, g->V_size, g->V_size));
     g->eval_h = (double *)calloc(vs, sizeof(double));
     g->res_h = (double *)calloc(3 * (nev + 8), sizeof(double));
