@@ -315,8 +315,12 @@ def run_gb300(args, dist):
         rows = roofline_from_profile(prof, hbm_peak, tensor_peak)
         dom = max(rows, key=lambda c: rows[c]["ms"])
         d = rows[dom]
-        traffic = load_traffic().get(dom)
         per_launch_alg = prof[dom]["bytes"] / max(prof[dom]["launches"], 1)
+        # ncu capture of one launch: measured / algorithmic DRAM bytes, applied to this
+        # solve's mean algorithmic bytes per launch of the class
+        cap = load_traffic().get(dom)
+        traffic = (cap["measured_bytes"] / cap["algorithmic_bytes"] * per_launch_alg
+                   if isinstance(cap, dict) else cap)
         spmm32 = rows.get("spmm_fp32")
         cpu = None
         if not args.no_cpu_baseline:
