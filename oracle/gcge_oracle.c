@@ -163,6 +163,7 @@ typedef struct {
     int nev, block_size, ev_max_it, cg_max_it, max_reorth_time, dirichlet, print_level;
     double ev_tol, cg_rate, orth_zero_tol, reorth_tol, scbgs_reorth_tol, criterion_tol;
     double multi_tol_for_lock, conv_omega_norm;
+    int opt_rr_eig_partly;
     char conv_type[4];
     /* para outputs */
     int num_unlock, num_iter;
@@ -455,21 +456,37 @@ static void rr_matrix(gcge_t *g, const csr_t *A)
 }
 
 /* GCGE_ComputeSubspaceEigenpairs, src/gcge_rayleighritz.c:364-590, single-process
- * path with opt_rr_eig_partly = 0 (so rr_eigen_start = 0): dsyevx("V","I","U")
- * for eigenpairs 1 .. min(max_dim_x, ldm) of a copy of the projected matrix. */
+ * path: with opt_rr_eig_partly the lock count is the first unconverged index,
+ * lowered by every earlier eigenvalue within multi_tol_for_lock of it
+ * (:378-394); the W columns' rows above it are zeroed in the projected matrix
+ * (:408-409), and dsyevx("V","I","U") solves the trailing block for the pairs
+ * lock+1 .. min(max_dim_x, ldm), writing eval and the coefficient columns from
+ * the lock count on (:522-546). Without it the lock count is 0. */
 static int rr_eig(gcge_t *g)
 {
     int ldm = g->dim_xpw;
     double *tmp = g->sub_dtmp, *work = tmp + (size_t)ldm * ldm;
     double vl = 0.0, vu = 0.0, abstol = 0.0;
-    int il = 1, iu = g->max_dim_x < ldm ? g->max_dim_x : ldm, m = iu - il + 1;
+    int start = g->opt_rr_eig_partly ? g->unlock[0] : 0;
+    int il = start;
+    for (int i = start - 1; i > -1; --i)
+        if (fabs(g->eval[i] - g->eval[start]) / g->eval[start] < g->multi_tol_for_lock) il -= 1;
+    start = il;
+    il += 1;
+    g->soft_locked = start;
+    int iu = g->max_dim_x < ldm ? g->max_dim_x : ldm, m = iu - il + 1;
     int lwork = 8 * ldm, info = 0, nrows = ldm, ncols = ldm;
     int *iwork = g->sub_itmp, *ifail = g->sub_itmp + 5 * ldm;
-    g->soft_locked = 0;
+    for (int i = 0; i < g->dim_xpw - g->dim_xp; ++i)
+        memset(g->sub_mat + (size_t)(g->dim_xp + i) * ldm, 0, (size_t)start * sizeof(double));
     memcpy(tmp, g->sub_mat, (size_t)ldm * ldm * sizeof(double));
+    nrows -= start;
+    il -= start;
+    iu -= start;
     char V = 'V', I = 'I', U = 'U';
-    scipy_dsyevx_(&V, &I, &U, &nrows, tmp, &ncols, &vl, &vu, &il, &iu, &abstol, &m,
-                  g->eval, g->sub_evec, &ldm, work, &lwork, iwork, ifail, &info);
+    scipy_dsyevx_(&V, &I, &U, &nrows, tmp + (size_t)start * ncols + start, &ncols, &vl, &vu, &il, &iu, &abstol, &m,
+                  g->eval + start, g->sub_evec + (size_t)start * ldm + start, &ldm, work, &lwork, iwork, ifail,
+                  &info);
     return info;
 }
 
@@ -644,6 +661,8 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
     g->block_size = p->block_size ? p->block_size : nev;
     g->ev_max_it = p->ev_max_it; g->cg_max_it = p->cg_max_it; g->max_reorth_time = p->max_reorth_time;
     g->dirichlet = p->dirichlet_boundary; g->print_level = p->print_level;
+    g->opt_rr_eig_partly = p->opt_rr_eig_partly;
+    g->multi_tol_for_lock = 1e-6;                 /* src/gcge_para.c:59 */
     g->ev_tol = p->ev_tol; g->cg_rate = p->cg_rate;
     g->orth_zero_tol = p->orth_zero_tol + DBL_EPSILON;
     g->reorth_tol = p->reorth_tol;
@@ -748,6 +767,11 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
         check_conv(g, A, B);
     }
 
+    /* the soft-locked Ritz vectors live in V: copied to evec at exit (src/gcge_eigsol.c:531-538) */
+    if (g->soft_locked > 0) {
+        int s[2] = {0, 0}, e[2] = {g->soft_locked, g->soft_locked};
+        mv_axpby(1.0, &g->V, 0.0, &g->evec, s, e);
+    }
     memcpy(eval_out, g->eval, sizeof(double) * nev);
     for (int j = 0; j < nev; ++j) memcpy(evec_out + (size_t)j * n, g->evec.c[j], sizeof(double) * n);
     clock_gettime(CLOCK_MONOTONIC, &t1);

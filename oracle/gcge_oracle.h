@@ -45,8 +45,8 @@ typedef struct {
                                    src/gcge_eigsol.c:448-472); the restatement keeps multi */
     char   orth_type[4];        /* reference build only: "A" orthonormalises in the A inner
                                    product (src/gcge_eigsol.c:100-113); "" = "B" */
-    int    opt_rr_eig_partly;   /* reference build only: soft locking in the Rayleigh-Ritz
-                                   eigensolve (src/gcge_rayleighritz.c:364-400)          */
+    int    opt_rr_eig_partly;   /* soft locking in the Rayleigh-Ritz eigensolve
+                                   (src/gcge_rayleighritz.c:364-400), restated too      */
 } gcge_oracle_params;
 
 typedef struct {
