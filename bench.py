@@ -536,7 +536,7 @@ def main():
     ap.add_argument("--max-it", type=int, default=400)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--fp64-warmup", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel", choices=["spmm_a", "spmm_b", "bcg32", "lincomb", "gram", "adjoint", "c3", "c5"],
                     help="time one hot operation instead of the solve (profiling)")
