@@ -164,6 +164,7 @@ typedef struct {
     double ev_tol, cg_rate, orth_zero_tol, reorth_tol, scbgs_reorth_tol, criterion_tol;
     double multi_tol_for_lock, conv_omega_norm;
     int opt_rr_eig_partly;
+    char w_orth_type[8];
     char conv_type[4];
     /* para outputs */
     int num_unlock, num_iter;
@@ -289,6 +290,56 @@ static int orth_plain(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
             mv_swap(V, V, s, e);
             end--;
             cur--;
+        }
+    }
+    return end;
+}
+
+/* GCGE_BOrthonormalization, src/gcge_orthogonal.c:352-528 (w_orth_type "bgs"):
+ * B V[:, 0:nev] into evec and B V[:, nev:dim_xp] into V_tmp once; then twice:
+ * W[:, start:end) projected against each of X and P in turn (classical per
+ * vector, V^T evec / V^T V_tmp), and W itself by modified Gram-Schmidt with its
+ * B-norm; a column of norm <= orth_zero_tol is swapped to the end and dropped. */
+static int bgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    const int n = V->n, nev = g->nev, dim_xp = g->dim_xp;
+    double *d = g->sub_dtmp;
+    for (int j = 0; j < nev; ++j) {
+        if (!B) vaxpby(n, 1.0, V->c[j], 0.0, g->evec.c[j]);
+        else csr_mv(B, V->c[j], g->evec.c[j]);
+    }
+    for (int j = nev; j < dim_xp; ++j) {
+        if (!B) vaxpby(n, 1.0, V->c[j], 0.0, g->V_tmp.c[j - nev]);
+        else csr_mv(B, V->c[j], g->V_tmp.c[j - nev]);
+    }
+    for (int i = 0; i < 2; ++i) {
+        int wl = end - start;
+        for (int cur = 0; cur < nev; ++cur) {
+            int s[2] = {start, cur}, e[2] = {end, cur + 1};
+            mv_inner(V, &g->evec, d, 0, s, e, wl);
+            for (int j = start; j < end; ++j) vaxpby(n, -d[j - start], V->c[cur], 1.0, V->c[j]);
+        }
+        for (int cur = nev; cur < dim_xp; ++cur) {
+            int s[2] = {start, cur - nev}, e[2] = {end, cur + 1 - nev};
+            mv_inner(V, &g->V_tmp, d, 0, s, e, wl);
+            for (int j = start; j < end; ++j) vaxpby(n, -d[j - start], V->c[cur], 1.0, V->c[j]);
+        }
+        for (int cur = start; cur < end; cur++) {
+            if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, g->CG_p.c[0]);
+            else csr_mv(B, V->c[cur], g->CG_p.c[0]);
+            int s[2] = {cur, 0}, e[2] = {end, 1};
+            wl = end - cur;
+            mv_inner(V, &g->CG_p, d, 0, s, e, wl);
+            const double nv = sqrt(d[0]);
+            if (nv > g->orth_zero_tol) {
+                vaxpby(n, 0.0, V->c[cur], 1.0 / nv, V->c[cur]);
+                for (int j = cur + 1; j < end; ++j) vaxpby(n, -d[j - cur] / nv, V->c[cur], 1.0, V->c[j]);
+            } else {
+                int s2[2] = {cur, end - 1}, e2[2] = {cur + 1, end};
+                mv_swap(V, V, s2, e2);
+                end--;
+                cur--;
+            }
         }
     }
     return end;
@@ -662,6 +713,7 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
     g->ev_max_it = p->ev_max_it; g->cg_max_it = p->cg_max_it; g->max_reorth_time = p->max_reorth_time;
     g->dirichlet = p->dirichlet_boundary; g->print_level = p->print_level;
     g->opt_rr_eig_partly = p->opt_rr_eig_partly;
+    strncpy(g->w_orth_type, p->w_orth_type[0] ? p->w_orth_type : "multi", 7);
     g->multi_tol_for_lock = 1e-6;                 /* src/gcge_para.c:59 */
     g->ev_tol = p->ev_tol; g->cg_rate = p->cg_rate;
     g->orth_zero_tol = p->orth_zero_tol + DBL_EPSILON;
@@ -758,7 +810,16 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
         compute_w(g, A, B);
         g->last_dim_xpw = g->dim_xpw;
         g->dim_xpw = g->dim_xp + g->unconv_bs;
-        g->dim_xpw = stable_multi_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
+        /* w_orth_type dispatch, src/gcge_eigsol.c:448-472 (cbgs / scbgs not restated) */
+        if (strcmp(g->w_orth_type, "multi") == 0)
+            g->dim_xpw = stable_multi_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
+        else if (strcmp(g->w_orth_type, "bgs") == 0)
+            g->dim_xpw = bgs_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
+        else if (strcmp(g->w_orth_type, "cbgs") == 0 || strcmp(g->w_orth_type, "scbgs") == 0) {
+            status = 4;
+            break;
+        } else
+            g->dim_xpw = orth_plain(g, &g->V, g->dim_xp, g->dim_xpw, B);
         rr_matrix(g, A);
         if (rr_eig(g)) status = 3;
         g->last_dim_x = g->dim_x;

@@ -41,8 +41,9 @@ typedef struct {
                                    1: counter-hash uniform [0,1) shared with the GPU    */
     unsigned long long seed;
     int    print_level;         /* 0 silent, 1 per-iteration line                       */
-    char   w_orth_type[8];      /* reference build only: GCGE's w_orth_type ("" = "multi";
-                                   src/gcge_eigsol.c:448-472); the restatement keeps multi */
+    char   w_orth_type[8];      /* GCGE's w_orth_type ("" = "multi"; src/gcge_eigsol.c:448-472):
+                                   the restatement covers multi, bgs and the fallback
+                                   GCGE_Orthonormalization; cbgs / scbgs return status 4 */
     char   orth_type[4];        /* reference build only: "A" orthonormalises in the A inner
                                    product (src/gcge_eigsol.c:100-113); "" = "B" */
     int    opt_rr_eig_partly;   /* soft locking in the Rayleigh-Ritz eigensolve
