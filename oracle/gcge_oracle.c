@@ -345,6 +345,68 @@ static int bgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
     return end;
 }
 
+/* GCGE_CBOrthonormalization, src/gcge_orthogonal.c:755-964 (w_orth_type "cbgs"):
+ * two block passes W -= V (V^T B W) against V[:, 0:start), then once: the Gram
+ * W^T B W, and if any entry exceeds orth_zero_tol its eigenpairs by dsyevx,
+ * eigenvectors of eigenvalues >= orth_zero_tol scaled by theta^-1/2 (everything up
+ * to the last smaller one dropped), W <- W Q (the linear combination's stride and
+ * offset use the reduced count, as the reference does), swapped into V. */
+static int cbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    const int n = V->n, w0 = end - start;
+    double *d = g->sub_dtmp, *tmp_evec = g->sub_evec, *tmp_eval = tmp_evec + (size_t)w0 * w0;
+    double *dwork = d + (size_t)w0 * w0;
+    int *iwork = g->sub_itmp, *ifail = g->sub_itmp + 5 * w0;
+    int wl = w0;
+    for (int i = 0; i < 2; ++i) {
+        wl = end - start;
+        int s[2] = {start, 0}, e[2] = {end, wl};
+        if (!B) mv_axpby(1.0, V, 0.0, &g->V_tmp, s, e);
+        else mv_matdot(B, V, &g->V_tmp, s, e);
+        int s1[2] = {0, 0}, e1[2] = {start, wl};
+        mv_inner(V, &g->V_tmp, d, 0, s1, e1, start);
+        mv_lincomb(V, &g->V_tmp, s1, e1, d, start);
+        int s2[2] = {0, start}, e2[2] = {wl, end};
+        mv_axpby(-1.0, &g->V_tmp, 1.0, V, s2, e2);
+    }
+    for (int j = 0; j < wl; ++j) {
+        if (!B) vaxpby(n, 1.0, V->c[j + start], 0.0, g->V_tmp.c[j]);
+        else csr_mv(B, V->c[j + start], g->V_tmp.c[j]);
+    }
+    {
+        int s[2] = {start, 0}, e[2] = {end, wl};
+        mv_inner(V, &g->V_tmp, d, 0, s, e, wl);
+    }
+    int nonzero = 0;
+    for (int j = 0; j < wl * wl; ++j)
+        if (d[j] > g->orth_zero_tol) {
+            nonzero = 1;
+            break;
+        }
+    if (!nonzero) return start;
+    double vl = 0.0, vu = 0.0, abstol = 0.0;
+    int il = 1, iu = wl, m = iu - il + 1, lwork = 8 * w0, info = 0, nn = wl;
+    char V_ = 'V', I_ = 'I', U_ = 'U';
+    scipy_dsyevx_(&V_, &I_, &U_, &nn, d, &nn, &vl, &vu, &il, &iu, &abstol, &m, tmp_eval, tmp_evec, &nn, dwork, &lwork,
+                  iwork, ifail, &info);
+    int nz = 0;
+    for (int j = 0; j < wl; ++j) {
+        if (tmp_eval[j] < g->orth_zero_tol) nz = j + 1;
+        else arr_scal(1.0 / sqrt(tmp_eval[j]), tmp_evec + (size_t)j * wl, wl);
+    }
+    wl -= nz;
+    {
+        int s[2] = {start, 0}, e[2] = {end, wl};
+        mv_lincomb(V, &g->V_tmp, s, e, tmp_evec + (size_t)nz * wl, wl);
+    }
+    end = start + wl;
+    {
+        int s[2] = {start, 0}, e[2] = {end, wl};
+        mv_swap(V, &g->V_tmp, s, e);
+    }
+    return end;
+}
+
 /* GCGE_SubOrthonormalization, src/gcge_orthogonal.c:1880-1929:
  * V2 -= V1 (V1^T B V2), Gram left in sub_dtmp (len1 x len2, ld len1). */
 static void sub_orth(gcge_t *g, mv_t *V, const int *s, const int *e, const csr_t *B)
@@ -810,12 +872,14 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
         compute_w(g, A, B);
         g->last_dim_xpw = g->dim_xpw;
         g->dim_xpw = g->dim_xp + g->unconv_bs;
-        /* w_orth_type dispatch, src/gcge_eigsol.c:448-472 (cbgs / scbgs not restated) */
+        /* w_orth_type dispatch, src/gcge_eigsol.c:448-472 (scbgs not restated) */
         if (strcmp(g->w_orth_type, "multi") == 0)
             g->dim_xpw = stable_multi_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
         else if (strcmp(g->w_orth_type, "bgs") == 0)
             g->dim_xpw = bgs_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
-        else if (strcmp(g->w_orth_type, "cbgs") == 0 || strcmp(g->w_orth_type, "scbgs") == 0) {
+        else if (strcmp(g->w_orth_type, "cbgs") == 0)
+            g->dim_xpw = cbgs_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
+        else if (strcmp(g->w_orth_type, "scbgs") == 0) {
             status = 4;
             break;
         } else

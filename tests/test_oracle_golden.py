@@ -157,3 +157,20 @@ def test_reference_a_orthogonal_mode_fails():
     A, B = case_matrices("fem33_nev10_dirichlet")
     ev, X, st = ref.solve(A, B, ref.params(**dict(g["params"], seed=1234, orth_type="A", ev_max_it=100)))
     assert not np.all(np.isfinite(ev))
+
+
+@pytest.mark.parametrize("name", ["fem33_nev10_dirichlet", "laplace30x20_nev12_block4", "femcube10_nev6_abs"])
+def test_oracle_cbgs_bitwise_vs_reference_build(oracle, name):
+    """w_orth_type "cbgs" restated: bit-identical to the reference build over 30
+    outer iterations, although neither converges with it."""
+    ref = pyoracle.reference()
+    if ref is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    g = G[name]
+    A, B = case_matrices(name)
+    kw = dict(g["params"], w_orth_type="cbgs", ev_max_it=30)
+    e1, X1, s1 = oracle.solve(A, B, oracle.params(**kw))
+    e2, X2, s2 = ref.solve(A, B, ref.params(**kw))
+    assert s1.num_iter == s2.num_iter and s1.num_unlock == s2.num_unlock
+    assert np.array_equal(e1, e2, equal_nan=True)
+    assert np.array_equal(X1, X2, equal_nan=True)
