@@ -407,6 +407,106 @@ static int cbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
     return end;
 }
 
+/* GCGE_SCBOrth_Minus, src/gcge_orthogonal.c:1116-1195: W[:, start:end) -= the
+ * projection onto V[:, dim_xp:start), repeated while the summed squares of the
+ * first (start - dim_xp) * w entries of the Gram buffer exceed scbgs_reorth_tol
+ * (the Gram is stored with leading dimension start, as the reference does) */
+static void scb_minus(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    const int wl = end - start, dim_xp = g->dim_xp, length = (start - dim_xp) * wl;
+    double *d = g->sub_dtmp, vi = 1.0;
+    int iter = 0;
+    while (vi > g->scbgs_reorth_tol) {
+        iter++;
+        int s[2] = {start, 0}, e[2] = {end, wl};
+        if (!B) mv_axpby(1.0, V, 0.0, &g->V_tmp, s, e);
+        else mv_matdot(B, V, &g->V_tmp, s, e);
+        int s1[2] = {dim_xp, 0}, e1[2] = {start, wl};
+        mv_inner(V, &g->V_tmp, d, 0, s1, e1, start);
+        vi = 0.0;
+        for (int i = 0; i < length; ++i) vi += d[i] * d[i];
+        vi = sqrt(vi);
+        mv_lincomb(V, &g->V_tmp, s1, e1, d, start);
+        int s2[2] = {0, start}, e2[2] = {wl, end};
+        mv_axpby(-1.0, &g->V_tmp, 1.0, V, s2, e2);
+        if (iter >= g->max_reorth_time) break;
+    }
+}
+
+/* GCGE_SCBOrth_Self, src/gcge_orthogonal.c:1196-1281: modified Gram-Schmidt in the
+ * B inner product within W[:, start:end), scbgs_wself_max_reorth_time (1) times */
+static int scb_self(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    const int n = V->n;
+    double *d = g->sub_dtmp;
+    for (int it = 0; it < 1; ++it) {
+        for (int cur = start; cur < end; cur++) {
+            if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, g->CG_p.c[0]);
+            else csr_mv(B, V->c[cur], g->CG_p.c[0]);
+            int s[2] = {cur, 0}, e[2] = {end, 1};
+            mv_inner(V, &g->CG_p, d, 0, s, e, end - cur);
+            const double nv = sqrt(d[0]);
+            if (nv > g->orth_zero_tol) {
+                vaxpby(n, 0.0, V->c[cur], 1.0 / nv, V->c[cur]);
+                for (int j = cur + 1; j < end; ++j) vaxpby(n, -d[j - cur] / nv, V->c[cur], 1.0, V->c[j]);
+            } else {
+                int s2[2] = {cur, end - 1}, e2[2] = {cur + 1, end};
+                mv_swap(V, V, s2, e2);
+                end--;
+                cur--;
+            }
+        }
+    }
+    return end;
+}
+
+/* GCGE_SCBOrthonormalization, src/gcge_orthogonal.c:967-1115 (w_orth_type
+ * "scbgs"): block projections of W against V[:, 0:start) while their norm exceeds
+ * scbgs_reorth_tol (at most max_reorth_time), then W in blocks of
+ * w_orth_block_size = max(block_size / 5, 1) (src/gcge_para.c:373-376): each block
+ * projected against the W columns before it and orthonormalised by itself; columns
+ * a block drops are swapped behind the remaining ones */
+static int scbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+{
+    const int w0 = end - start, length = start * w0;
+    double *d = g->sub_dtmp, vi = 1.0;
+    int iter = 0;
+    while (vi > g->scbgs_reorth_tol) {
+        iter++;
+        int s[2] = {start, 0}, e[2] = {end, w0};
+        if (!B) mv_axpby(1.0, V, 0.0, &g->V_tmp, s, e);
+        else mv_matdot(B, V, &g->V_tmp, s, e);
+        int s1[2] = {0, 0}, e1[2] = {start, w0};
+        mv_inner(V, &g->V_tmp, d, 0, s1, e1, start);
+        vi = 0.0;
+        for (int i = 0; i < length; ++i) vi += d[i] * d[i];
+        vi = sqrt(vi);
+        mv_lincomb(V, &g->V_tmp, s1, e1, d, start);
+        int s2[2] = {0, start}, e2[2] = {w0, end};
+        mv_axpby(-1.0, &g->V_tmp, 1.0, V, s2, e2);
+        if (iter >= g->max_reorth_time) break;
+    }
+    const int bsz = g->block_size / 5 > 1 ? g->block_size / 5 : 1;
+    const int step = (end - start) < bsz ? (end - start) : bsz;
+    int ws = start, we = ws + step;
+    if (we > end) we = end;
+    we = scb_self(g, V, ws, we, B);
+    while (we < end) {
+        ws = we;
+        we = ws + step;
+        if (we > end) we = end;
+        const int old_we = we;
+        scb_minus(g, V, ws, we, B);
+        we = scb_self(g, V, ws, we, B);
+        if (we < old_we) {
+            end -= old_we - we;
+            int s2[2] = {we, end}, e2[2] = {old_we, end + old_we - we};
+            mv_swap(V, V, s2, e2);
+        }
+    }
+    return end;
+}
+
 /* GCGE_SubOrthonormalization, src/gcge_orthogonal.c:1880-1929:
  * V2 -= V1 (V1^T B V2), Gram left in sub_dtmp (len1 x len2, ld len1). */
 static void sub_orth(gcge_t *g, mv_t *V, const int *s, const int *e, const csr_t *B)
@@ -872,17 +972,16 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
         compute_w(g, A, B);
         g->last_dim_xpw = g->dim_xpw;
         g->dim_xpw = g->dim_xp + g->unconv_bs;
-        /* w_orth_type dispatch, src/gcge_eigsol.c:448-472 (scbgs not restated) */
+        /* w_orth_type dispatch, src/gcge_eigsol.c:448-472 */
         if (strcmp(g->w_orth_type, "multi") == 0)
             g->dim_xpw = stable_multi_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
         else if (strcmp(g->w_orth_type, "bgs") == 0)
             g->dim_xpw = bgs_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
         else if (strcmp(g->w_orth_type, "cbgs") == 0)
             g->dim_xpw = cbgs_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
-        else if (strcmp(g->w_orth_type, "scbgs") == 0) {
-            status = 4;
-            break;
-        } else
+        else if (strcmp(g->w_orth_type, "scbgs") == 0)
+            g->dim_xpw = scbgs_orth(g, &g->V, g->dim_xp, g->dim_xpw, B);
+        else
             g->dim_xpw = orth_plain(g, &g->V, g->dim_xp, g->dim_xpw, B);
         rr_matrix(g, A);
         if (rr_eig(g)) status = 3;

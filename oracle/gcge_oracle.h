@@ -42,8 +42,8 @@ typedef struct {
     unsigned long long seed;
     int    print_level;         /* 0 silent, 1 per-iteration line                       */
     char   w_orth_type[8];      /* GCGE's w_orth_type ("" = "multi"; src/gcge_eigsol.c:448-472):
-                                   the restatement covers multi, bgs, cbgs and the
-                                   fallback GCGE_Orthonormalization; scbgs returns status 4 */
+                                   every variant is restated (multi, bgs, cbgs, scbgs,
+                                   the fallback GCGE_Orthonormalization)                */
     char   orth_type[4];        /* reference build only: "A" orthonormalises in the A inner
                                    product (src/gcge_eigsol.c:100-113); "" = "B" */
     int    opt_rr_eig_partly;   /* soft locking in the Rayleigh-Ritz eigensolve

@@ -34,13 +34,14 @@ def test_oracle_matches_reference_golden(oracle, name):
     np.testing.assert_allclose(np.linalg.norm(X, axis=0), g["evec_colnorm"], rtol=1e-12)
 
 
-@pytest.mark.parametrize("soft_lock,w_orth_type", [(0, "multi"), (1, "multi"), (0, "bgs"), (0, "gs"), (1, "bgs")])
+@pytest.mark.parametrize("soft_lock,w_orth_type", [(0, "multi"), (1, "multi"), (0, "bgs"), (0, "gs"), (1, "bgs"),
+                                                   (0, "scbgs"), (1, "scbgs")])
 @pytest.mark.parametrize("name", ["fem33_nev10_dirichlet", "laplace30x20_nev12_block4", "laplace100_nev10",
                                   "femcube10_nev6_abs"])
 def test_oracle_bitwise_vs_reference_build(oracle, name, soft_lock, w_orth_type):
     """The restatement and the reference build agree bit for bit: default
     Rayleigh-Ritz step or soft locking (opt_rr_eig_partly = 1); W orthonormalised by
-    the default, by bgs, or by the fallback GCGE_Orthonormalization ("gs")."""
+    the default, by bgs, by scbgs, or by the fallback GCGE_Orthonormalization ("gs")."""
     ref = pyoracle.reference()
     if ref is None:
         pytest.skip("reference build (oracle/_ref) not present")
