@@ -41,7 +41,7 @@ WORKLOADS = {
     "fem48": (48, 50, 64),
     "fem24": (24, 20, 24),
 }
-HW_FP64_TFLOPS = 1.199   # FP64 FMA throughput measured on a GB300 (gcge-1.0_gb300/csrc/probe_throughput.cu)
+HW_FP64_TFLOPS = 1.199   # FP64 FMA throughput measured on a GB300 (profiles/gb300_throughput_probe.md)
 HW_FP32_TOPS = 35.0      # FP32 FMA-pipe instructions per second x 1e-12 (70.0 TFLOP/s, the same probe)
 PAIR_OPS = 13            # FP32 operations per (nonzero, column) of the FP32-pair SpMM
 

@@ -9,7 +9,7 @@
 // The active set follows the reference exactly: after each round the count of
 // columns whose residual ratio ||r_k||/||r_0|| is still >= cg_rate is taken
 // over all columns, and the next round updates the first `count` columns
-// (src/gcge_cg.c:713-720 writes unlock[idx] = idx at position idx, and the
+// (src/gcge_cg.c:286-294 writes unlock[idx] = idx at position idx, and the
 // update loops walk unlock[0 .. num_unlock)).
 //
 // precision 0: FP64 vectors and values. precision 1: the residual of the initial
@@ -191,7 +191,7 @@ __global__ void k_finalize(int k, const double *__restrict__ sums, double *rho1,
             const double s = sums[c];
             rho1[c] = rho2[c];
             rho2[c] = s;
-            beta[c] = s / rho1[c];   // the next round's beta (src/gcge_cg.c:645)
+            beta[c] = s / rho1[c];   // the next round's beta (src/gcge_cg.c:219)
         }
         const double lerr = sqrt(fabs(rho2[c]));
         if (lerr / err[c] >= rate) atomicAdd(&cnt, 1);
@@ -518,7 +518,7 @@ k_colsum_finalize(int nblk, int k, const double *__restrict__ part, double *sums
             const double s = sums[c];
             rho1[c] = rho2[c];
             rho2[c] = s;
-            beta[c] = s / rho1[c];   // the next round's beta (src/gcge_cg.c:645)
+            beta[c] = s / rho1[c];   // the next round's beta (src/gcge_cg.c:219)
         }
         const double lerr = sqrt(fabs(rho2[c]));
         if (lerr / err[c] >= rate) atomicAdd(&cnt, 1);

@@ -16,7 +16,15 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# The reference source tree this recipe compiles from: GCGE_REFERENCE_ROOT when set,
+# else the read-only checkout of the build container. This recipe is the one place
+# that names it; tests and fixture scripts ask reference_root() below.
 REF_ROOT = os.environ.get("GCGE_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root():
+    """The reference source tree, or None where it is absent (as on the GPU host)."""
+    return REF_ROOT if os.path.isdir(os.path.join(REF_ROOT, "src")) else None
 REF_SOURCES = [
     "src/gcge_cg.c", "src/gcge_eigsol.c", "src/gcge_ops.c", "src/gcge_orthogonal.c",
     "src/gcge_para.c", "src/gcge_rayleighritz.c", "src/gcge_solver.c", "src/gcge_statistics.c",

@@ -23,7 +23,11 @@ sys.path.insert(0, os.path.join(ROOT, "gcge-1.0_gb300"))
 import pyoracle  # noqa: E402
 from gcge_gb300 import problems as P  # noqa: E402
 
-REF_DATA = os.environ.get("GCGE_REFERENCE_ROOT", "/root/reference") + "/test/data"
+import build_oracle  # noqa: E402  (the oracle recipe knows where the reference sources are)
+
+if build_oracle.reference_root() is None:
+    sys.exit("reference source tree absent: set GCGE_REFERENCE_ROOT to a GCGE-1.0 checkout")
+REF_DATA = os.path.join(build_oracle.reference_root(), "test", "data")
 
 
 def save_csr(path, M):

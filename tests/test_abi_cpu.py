@@ -4,13 +4,19 @@ GCGE_OPS layout restated in include/gcge_gb300_ops.h matches the reference's."""
 import ctypes as C
 import os
 import subprocess
+import sys
 
 import pytest
 
 import gcge_gb300 as G
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("GCGE_REFERENCE_ROOT", "/root/reference")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+if ORACLE_DIR not in sys.path:
+    sys.path.insert(0, ORACLE_DIR)
+import build_oracle  # noqa: E402  (the oracle recipe knows where the reference sources are)
+
+REF = build_oracle.reference_root()
 
 
 def has_gpu():
@@ -50,7 +56,7 @@ def test_null_arguments_rejected():
     assert L.GCGE_GPU_SetOps(None, None) == 1
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree absent")
+@pytest.mark.skipif(REF is None, reason="reference source tree absent (set GCGE_REFERENCE_ROOT to a GCGE-1.0 checkout)")
 def test_ops_layout_matches_reference(tmp_path):
     cmd = ["gcc", "-std=gnu99", "-c", "-o", str(tmp_path / "x.o"), "-include", os.path.join(ROOT, "oracle", "ref_config.h"),
            "-I" + os.path.join(REF, "src"), "-I" + os.path.join(ROOT, "include"),

@@ -21,8 +21,12 @@ def test_no_alloc_gram_matches_allocating_entry_point():
     ctx = G.Context(0)
     lib = ctx.lib
     rng = np.random.default_rng(21)
-    cases = [(200003, 40, 40, True), (150000, 33, 17, False), (4099, 96, 80, False)]
-    for n, k1, k2, sym in cases:
+    # the last case has k1 * k2 = 262,144, the largest the fixed array takes (room
+    # for four row splits of partials; the SM count asks for two at that size)
+    cases = [(200003, 40, 40, True, False), (150000, 33, 17, False, True), (4099, 96, 80, False, False),
+             (300007, 512, 512, False, True)]
+    side = torch.cuda.Stream()
+    for n, k1, k2, sym, on_side in cases:
         ldv, ldw, lda = k1 + 3, k2 + 1, k1 + 2
         V = rng.standard_normal((n, ldv))
         W = rng.standard_normal((n, ldw))
@@ -33,10 +37,18 @@ def test_no_alloc_gram_matches_allocating_entry_point():
         scale = np.max(np.abs(ref))
         tV = torch.from_numpy(V).cuda()
         tW = torch.from_numpy(W).cuda()
+        del V, W
         for _ in range(2):
             ta = torch.full((k2, lda), float("nan"), dtype=torch.float64, device="cuda")
-            st = lib.GCGE_GPU_InnerProdNoAlloc(n, k1, k2, tV.data_ptr(), ldv, tW.data_ptr(), ldw, ta.data_ptr(),
-                                               lda, int(sym), None)
+            if on_side:
+                # the caller's own stream: the call is ordered on it and on nothing else
+                side.wait_stream(torch.cuda.current_stream())
+                st = lib.GCGE_GPU_InnerProdNoAlloc(n, k1, k2, tV.data_ptr(), ldv, tW.data_ptr(), ldw,
+                                                   ta.data_ptr(), lda, int(sym), side.cuda_stream)
+                side.synchronize()
+            else:
+                st = lib.GCGE_GPU_InnerProdNoAlloc(n, k1, k2, tV.data_ptr(), ldv, tW.data_ptr(), ldw,
+                                                   ta.data_ptr(), lda, int(sym), None)
             assert st == 0
             torch.cuda.synchronize()
             got = ta.cpu().numpy().ravel()
@@ -44,6 +56,7 @@ def test_no_alloc_gram_matches_allocating_entry_point():
                 np.testing.assert_allclose(got[j * lda:j * lda + k1], ref[j * lda:j * lda + k1], rtol=1e-12,
                                            atol=1e-12 * scale)
                 assert np.all(np.isnan(got[j * lda + k1:(j + 1) * lda]))   # padding rows untouched
+        del tV, tW, mv_v, mv_w
     # sizes beyond the fixed array are rejected before any launch
     small = torch.zeros(16, dtype=torch.float64, device="cuda")
     assert lib.GCGE_GPU_InnerProdNoAlloc(1000, 600, 600, small.data_ptr(), 600, small.data_ptr(), 600,
