@@ -53,11 +53,13 @@ def _newer(target, deps):
 def build_oracle(verbose=False):
     out = os.path.join(HERE, "libgcge_oracle.so")
     src = os.path.join(HERE, "gcge_oracle.c")
-    deps = [src, os.path.join(HERE, "gcge_oracle.h"), __file__]
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    deps = [src, os.path.join(HERE, "gcge_oracle.h"), os.path.join(inc, "gcge_gb300_ops.h"),
+            os.path.join(inc, "gcge_gb300.h"), __file__]
     if _newer(out, deps):
         return out
     d, f = openblas()
-    cmd = ["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-o", out, src,
+    cmd = ["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-Wall", "-o", out, src, "-I" + inc,
            "-L" + d, "-l:" + f, "-Wl,-rpath," + d, "-lm"]
     if verbose:
         print(" ".join(cmd))

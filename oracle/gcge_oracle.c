@@ -22,6 +22,7 @@
 #include <time.h>
 
 #include "gcge_oracle.h"
+#include "gcge_gb300_ops.h"
 
 /* ------------------------------------------------------------------ LAPACK */
 extern void scipy_dsyevx_(char *jobz, char *range, char *uplo, int *n, double *a, int *lda,
@@ -47,11 +48,26 @@ static void dgemm(char ta, char tb, int m, int n, int k, double alpha, double *a
 }
 
 /* --------------------------------------------------------------- CSR ops */
+/* Every n-sized operation of the restatement goes through a table with the
+ * GCGE_OPS layout (src/gcge_ops.h:29-215), as the reference's solver core does.
+ * The default table below is the CSR backend of the reference (host arrays,
+ * app/csr/gcge_app_csr.c:70-84, with the multivector defaults of
+ * src/gcge_ops.c:115-300); gcge_oracle_solve_table runs the same restatement
+ * over a caller's table (GCGE's core driving another backend). */
+typedef GCGE_GPU_OPS_LAYOUT ops_t;
+static ops_t *T;                  /* the table the current call goes through */
+
 typedef struct { int n; const int *rp, *ci; const double *v; } csr_t;
+/* CSR_VEC, app/csr/gcge_app_csr.h:42-46: a size and its entries */
+typedef struct { int size; double *e; } hvec_t;
+static double *hcol(void *v) { return ((hvec_t *)v)->e; }
 
 /* app/csr/gcge_app_csr.c:297-323: zero y, then accumulate row by row */
-static void csr_mv(const csr_t *A, const double *x, double *y)
+static void h_matvec(void *mat, void *xv, void *yv)
 {
+    const csr_t *A = (const csr_t *)mat;
+    const double *x = hcol(xv);
+    double *y = hcol(yv);
     memset(y, 0, (size_t)A->n * sizeof(double));
     for (int i = 0; i < A->n; ++i)
         for (int j = A->rp[i]; j < A->rp[i + 1]; ++j)
@@ -59,8 +75,11 @@ static void csr_mv(const csr_t *A, const double *x, double *y)
 }
 
 /* app/csr/gcge_app_csr.c:330-365: y = a x + b y with its three special cases */
-static void vaxpby(int n, double a, const double *x, double b, double *y)
+static void h_axpby(double a, void *xv, double b, void *yv)
 {
+    const int n = ((hvec_t *)yv)->size;
+    const double *x = hcol(xv);
+    double *y = hcol(yv);
     if (a == 0.0) {
         for (int i = 0; i < n; ++i) y[i] = b * y[i];
     } else if (b == 0.0) {
@@ -72,11 +91,23 @@ static void vaxpby(int n, double a, const double *x, double b, double *y)
 }
 
 /* app/csr/gcge_app_csr.c:368-378 */
-static double vdot(int n, const double *x, const double *y)
+static void h_dot(void *xv, void *yv, double *value)
 {
+    const int n = ((hvec_t *)xv)->size;
+    const double *x = hcol(xv), *y = hcol(yv);
     double s = 0.0;
     for (int i = 0; i < n; ++i) s += x[i] * y[i];
-    return s;
+    *value = s;
+}
+
+/* the operations the restatement uses, each one table call */
+static void csr_mv(void *A, void *x, void *y) { T->MatDotVec(A, x, y); }
+static void vaxpby(double a, void *x, double b, void *y) { T->VecAxpby(a, x, b, y); }
+static double vdot(void *x, void *y)
+{
+    double v = 0.0;
+    T->VecInnerProd(x, y, &v);
+    return v;
 }
 
 /* counter hash shared with the GPU solver's initial vectors (splitmix64 finaliser) */
@@ -91,47 +122,74 @@ double gcge_oracle_hash_uniform(unsigned long long seed, unsigned long long inde
 }
 
 /* ----------------------------------------------------------- multivector */
-/* An ordered set of columns; the reference's void** multivector. */
-typedef struct { int n, k; double **c; double *store; } mv_t;
+/* An ordered set of column handles; the reference's void** multivector. */
+typedef struct { int n, k; void **c; hvec_t *vecs; double *store; } mv_t;
 
-static void mv_alloc(mv_t *m, int n, int k)
+/* host columns over caller storage (base == NULL: owned, zeroed) */
+static void h_mv_make(mv_t *m, int n, int k, double *base)
 {
     m->n = n; m->k = k;
-    m->store = (double *)calloc((size_t)n * (k > 0 ? k : 1), sizeof(double));
-    m->c = (double **)malloc(sizeof(double *) * (k > 0 ? k : 1));
-    for (int j = 0; j < k; ++j) m->c[j] = m->store + (size_t)j * n;
+    m->store = base ? NULL : (double *)calloc((size_t)n * (k > 0 ? k : 1), sizeof(double));
+    m->vecs = (hvec_t *)malloc(sizeof(hvec_t) * (k > 0 ? k : 1));
+    m->c = (void **)malloc(sizeof(void *) * (k > 0 ? k : 1));
+    for (int j = 0; j < k; ++j) {
+        m->vecs[j].size = n;
+        m->vecs[j].e = (base ? base : m->store) + (size_t)j * n;
+        m->c[j] = &m->vecs[j];
+    }
 }
-static void mv_free(mv_t *m) { free(m->store); free(m->c); m->store = NULL; m->c = NULL; }
+static void h_mv_free(mv_t *m)
+{
+    free(m->store); free(m->vecs); free(m->c);
+    m->store = NULL; m->vecs = NULL; m->c = NULL;
+}
+
+/* the restatement's workspace: GCGE_WORKSPACE_Setup creates it through
+ * ops->MultiVecCreateByMat (src/gcge_workspace.c:76-78) */
+static int g_host;   /* 1: the current call runs on the host table */
+static void mv_alloc(mv_t *m, void *mat, int n, int k)
+{
+    if (g_host) { h_mv_make(m, n, k, NULL); return; }
+    m->n = n; m->k = k; m->vecs = NULL; m->store = NULL; m->c = NULL;
+    T->MultiVecCreateByMat(&m->c, k, mat, T);
+}
+static void mv_free(mv_t *m)
+{
+    if (g_host) { h_mv_free(m); return; }
+    if (m->c) T->MultiVecDestroy(&m->c, m->k, T);
+    m->c = NULL;
+}
 
 /* src/gcge_ops.c:115-129 */
-static void mv_matdot(const csr_t *A, mv_t *x, mv_t *y, const int *s, const int *e)
+static void h_mv_matdot(void *A, void **x, void **y, int *s, int *e, ops_t *ops)
 {
-    for (int i = 0; i < e[0] - s[0]; ++i) csr_mv(A, x->c[s[0] + i], y->c[s[1] + i]);
+    for (int i = 0; i < e[0] - s[0]; ++i) ops->MatDotVec(A, x[s[0] + i], y[s[1] + i]);
 }
 /* src/gcge_ops.c:132-146 */
-static void mv_axpby(double a, mv_t *x, double b, mv_t *y, const int *s, const int *e)
+static void h_mv_axpby(double a, void **x, double b, void **y, int *s, int *e, ops_t *ops)
 {
-    for (int i = 0; i < e[0] - s[0]; ++i) vaxpby(x->n, a, x->c[s[0] + i], b, y->c[s[1] + i]);
+    for (int i = 0; i < e[0] - s[0]; ++i) ops->VecAxpby(a, x[s[0] + i], b, y[s[1] + i]);
 }
 /* src/gcge_ops.c:163-193: first column by a*x + 0*y, the rest accumulated with b = 1 */
-static void mv_lincomb(mv_t *x, mv_t *y, const int *s, const int *e, const double *a, int lda)
+static void h_mv_lincomb(void **x, void **y, int *s, int *e, double *a, int lda, void *dmat, int lddmat, ops_t *ops)
 {
+    (void)dmat; (void)lddmat;
     for (int jy = s[1]; jy < e[1]; ++jy) {
         const double *col = a + (size_t)(jy - s[1]) * lda;
-        vaxpby(x->n, col[0], x->c[s[0]], 0.0, y->c[jy]);
+        ops->VecAxpby(col[0], x[s[0]], 0.0, y[jy]);
         for (int ix = s[0] + 1; ix < e[0]; ++ix)
-            vaxpby(x->n, col[ix - s[0]], x->c[ix], 1.0, y->c[jy]);
+            ops->VecAxpby(col[ix - s[0]], x[ix], 1.0, y[jy]);
     }
 }
 /* src/gcge_ops.c:198-261 (MPI reduction omitted: one process) */
-static void mv_inner(mv_t *V, mv_t *W, double *a, int sym, const int *s, const int *e, int lda)
+static void h_mv_inner(void **V, void **W, double *a, char *is_sym, int *s, int *e, int lda, ops_t *ops)
 {
-    if (sym) {
+    if (strcmp(is_sym, "sym") == 0) {
         int len = e[1] - s[1];
         double *p = a;
         for (int iw = 0; iw < len; ++iw) {
             for (int iv = 0; iv <= iw; ++iv, ++p)
-                *p = vdot(V->n, V->c[iv + s[0]], W->c[iw + s[1]]);
+                ops->VecInnerProd(V[iv + s[0]], W[iw + s[1]], p);
             p += lda - (iw + 1);
         }
         for (int iw = 0; iw < len; ++iw)
@@ -142,20 +200,120 @@ static void mv_inner(mv_t *V, mv_t *W, double *a, int sym, const int *s, const i
         double *p = a;
         for (int iw = s[1]; iw < e[1]; ++iw) {
             for (int iv = s[0]; iv < e[0]; ++iv, ++p)
-                *p = vdot(V->n, V->c[iv], W->c[iw]);
+                ops->VecInnerProd(V[iv], W[iw], p);
             p += skip;
         }
     }
 }
-/* src/gcge_ops.c:285-300: exchange column pointers */
-static void mv_swap(mv_t *a, mv_t *b, const int *s, const int *e)
+/* src/gcge_ops.c:285-300: exchange column handles */
+static void h_mv_swap(void **a, void **b, int *s, int *e, ops_t *ops)
 {
+    (void)ops;
     for (int i = 0; i < e[0] - s[0]; ++i) {
-        double *t = a->c[s[0] + i];
-        a->c[s[0] + i] = b->c[s[1] + i];
-        b->c[s[1] + i] = t;
+        void *t = a[s[0] + i];
+        a[s[0] + i] = b[s[1] + i];
+        b[s[1] + i] = t;
     }
 }
+
+static void mv_matdot(void *A, mv_t *x, mv_t *y, const int *s, const int *e)
+{
+    int ss[2] = {s[0], s[1]}, ee[2] = {e[0], e[1]};
+    T->MatDotMultiVec(A, x->c, y->c, ss, ee, T);
+}
+static void mv_axpby(double a, mv_t *x, double b, mv_t *y, const int *s, const int *e)
+{
+    int ss[2] = {s[0], s[1]}, ee[2] = {e[0], e[1]};
+    T->MultiVecAxpby(a, x->c, b, y->c, ss, ee, T);
+}
+static void mv_lincomb(mv_t *x, mv_t *y, const int *s, const int *e, const double *a, int lda)
+{
+    int ss[2] = {s[0], s[1]}, ee[2] = {e[0], e[1]};
+    T->MultiVecLinearComb(x->c, y->c, ss, ee, (double *)a, lda, NULL, 0, T);
+}
+static void mv_inner(mv_t *V, mv_t *W, double *a, int sym, const int *s, const int *e, int lda)
+{
+    int ss[2] = {s[0], s[1]}, ee[2] = {e[0], e[1]};
+    char sy[] = "sym", ns[] = "nonsym";
+    T->MultiVecInnerProd(V->c, W->c, a, sym ? sy : ns, ss, ee, lda, T);
+}
+static void mv_swap(mv_t *a, mv_t *b, const int *s, const int *e)
+{
+    int ss[2] = {s[0], s[1]}, ee[2] = {e[0], e[1]};
+    T->MultiVecSwap(a->c, b->c, ss, ee, T);
+}
+
+/* dsyevx("V", "I", "U") of the projected problems, ops->DenseMatEigenSolver
+ * (default src/gcge_ops.c:302-316) */
+static void h_dsyevx(char *jobz, char *range, char *uplo, int *nrows, double *a, int *lda, double *vl, double *vu,
+                     int *il, int *iu, double *abstol, int *nev, double *eval, double *evec, int *lde, int *isuppz,
+                     double *work, int *lwork, int *iwork, int *liwork, int *ifail, int *info)
+{
+    (void)isuppz; (void)liwork;
+    scipy_dsyevx_(jobz, range, uplo, nrows, a, lda, vl, vu, il, iu, abstol, nev, eval, evec, lde, work, lwork, iwork,
+                  ifail, info);
+}
+static void dsyevx(char *jobz, char *range, char *uplo, int *nrows, double *a, int *lda, double *vl, double *vu,
+                   int *il, int *iu, double *abstol, int *nev, double *eval, double *evec, int *lde, double *work,
+                   int *lwork, int *iwork, int *ifail, int *info)
+{
+    int liwork = 0;
+    T->DenseMatEigenSolver(jobz, range, uplo, nrows, a, lda, vl, vu, il, iu, abstol, nev, eval, evec, lde, NULL, work,
+                           lwork, iwork, &liwork, ifail, info);
+}
+
+static void h_dirichlet(void **vecs, int nev, void *Av, void *Bv);
+
+/* CSR_VecSetRandomValue, app/csr/gcge_app_csr.c:283-293: libc rand() / (RAND_MAX + 1) */
+static void h_vec_random(void *v)
+{
+    hvec_t *x = (hvec_t *)v;
+    for (int i = 0; i < x->size; ++i) x->e[i] = ((double)rand()) / ((double)RAND_MAX + 1);
+}
+/* GCGE_Default_MultiVecSetRandomValue, src/gcge_ops.c:102-112: column by column */
+static void h_mv_random(void **mv, int start, int n_vec, ops_t *ops)
+{
+    for (int i = 0; i < n_vec; ++i) ops->VecSetRandomValue(mv[start + i]);
+}
+/* GCGE_Default_MultiVecCreateByMat / Destroy, src/gcge_ops.c:72-100: one vector
+ * (its own storage) per handle, so that handles exchanged between multivectors
+ * are each freed once, by whichever multivector holds them at the end */
+static void h_mv_create_by_mat(void ***mv, int k, void *mat, ops_t *ops)
+{
+    (void)ops;
+    const int n = ((const csr_t *)mat)->n;
+    void **h = (void **)malloc(sizeof(void *) * (k > 0 ? k : 1));
+    for (int j = 0; j < k; ++j) {
+        hvec_t *v = (hvec_t *)malloc(sizeof(hvec_t));
+        v->size = n;
+        v->e = (double *)calloc((size_t)n, sizeof(double));
+        h[j] = v;
+    }
+    *mv = h;
+}
+static void h_mv_destroy(void ***mv, int k, ops_t *ops)
+{
+    (void)ops;
+    if (!mv || !*mv) return;
+    for (int j = 0; j < k; ++j) {
+        hvec_t *v = (hvec_t *)(*mv)[j];
+        if (v) { free(v->e); free(v); }
+    }
+    free(*mv);
+    *mv = NULL;
+}
+
+/* the reference's CSR table (GCGE_CSR_SetOps, app/csr/gcge_app_csr.c:70-84, plus the
+ * defaults GCGE_OPS_Setup installs, src/gcge_ops.c:521-604) */
+static ops_t H_OPS = {
+    .MatDotVec = h_matvec, .VecAxpby = h_axpby, .VecInnerProd = h_dot, .VecLocalInnerProd = h_dot,
+    .MatDotMultiVec = h_mv_matdot, .MultiVecAxpby = h_mv_axpby, .MultiVecLinearComb = h_mv_lincomb,
+    .MultiVecInnerProd = h_mv_inner, .MultiVecSwap = h_mv_swap, .DenseMatEigenSolver = h_dsyevx,
+    .SetDirichletBoundary = h_dirichlet, .VecSetRandomValue = h_vec_random, .MultiVecSetRandomValue = h_mv_random,
+    .MultiVecCreateByMat = h_mv_create_by_mat, .MultiVecDestroy = h_mv_destroy,
+};
+
+static void use_host_table(void) { T = &H_OPS; g_host = 1; }
 
 /* ------------------------------------------------------------------ state */
 typedef struct {
@@ -176,7 +334,7 @@ typedef struct {
     int *unlock;
     double *eval, *sub_dtmp, *sub_evec, *sub_mat;
     int *sub_itmp;
-    const csr_t *A, *B;
+    void *A, *B;
 } gcge_t;
 
 /* ------------------------------------------------------- block CG (a8) */
@@ -184,16 +342,15 @@ typedef struct {
  * CG_X = X[:, xs : xs+len]. The active list is rebuilt each iteration by writing
  * unlock[idx] = idx at position idx (src/gcge_cg.c:713-720), so the update loops,
  * which walk unlock[0 .. num_unlock), always touch the first num_unlock columns. */
-static void bcg(const csr_t *A, mv_t *R, mv_t *X, int xs, int len, mv_t *P, mv_t *Wk,
+static void bcg(void *A, mv_t *R, mv_t *X, int xs, int len, mv_t *P, mv_t *Wk,
                 double *dtmp, int *itmp, int cg_max_it, double rate)
 {
-    int n = A->n;
     double *rho1 = dtmp, *rho2 = rho1 + len, *err = rho2 + len, *lerr = err + len, *ptw = lerr + len;
     int *unlock = itmp, num_unlock = 0;
     for (int idx = 0; idx < len; ++idx) {
         csr_mv(A, X->c[xs + idx], Wk->c[idx]);
-        vaxpby(n, -1.0, Wk->c[idx], 1.0, R->c[idx]);
-        rho2[idx] = vdot(n, R->c[idx], R->c[idx]);
+        vaxpby(-1.0, Wk->c[idx], 1.0, R->c[idx]);
+        rho2[idx] = vdot(R->c[idx], R->c[idx]);
         unlock[idx] = idx;
         num_unlock++;
     }
@@ -203,27 +360,27 @@ static void bcg(const csr_t *A, mv_t *R, mv_t *X, int xs, int len, mv_t *P, mv_t
         if (niter == 1) {
             for (int id = 0; id < num_unlock; ++id) {
                 int idx = unlock[id];
-                vaxpby(n, 1.0, R->c[idx], 0.0, P->c[idx]);
+                vaxpby(1.0, R->c[idx], 0.0, P->c[idx]);
             }
         } else {
             for (int id = 0; id < num_unlock; ++id) {
                 int idx = unlock[id];
                 double beta = rho2[idx] / rho1[idx];
-                vaxpby(n, 1.0, R->c[idx], beta, P->c[idx]);
+                vaxpby(1.0, R->c[idx], beta, P->c[idx]);
             }
         }
         for (int id = 0; id < num_unlock; ++id) {
             int idx = unlock[id];
             csr_mv(A, P->c[idx], Wk->c[idx]);
-            ptw[idx] = vdot(n, P->c[idx], Wk->c[idx]);
+            ptw[idx] = vdot(P->c[idx], Wk->c[idx]);
         }
         for (int id = 0; id < num_unlock; ++id) {
             int idx = unlock[id];
             double alpha = rho2[idx] / ptw[idx];
-            vaxpby(n, alpha, P->c[idx], 1.0, X->c[xs + idx]);
-            vaxpby(n, -alpha, Wk->c[idx], 1.0, R->c[idx]);
+            vaxpby(alpha, P->c[idx], 1.0, X->c[xs + idx]);
+            vaxpby(-alpha, Wk->c[idx], 1.0, R->c[idx]);
             rho1[idx] = rho2[idx];
-            rho2[idx] = vdot(n, R->c[idx], R->c[idx]);
+            rho2[idx] = vdot(R->c[idx], R->c[idx]);
         }
         for (int idx = 0; idx < len; ++idx) lerr[idx] = sqrt(fabs(rho2[idx]));
         num_unlock = 0;
@@ -237,29 +394,28 @@ static void bcg(const csr_t *A, mv_t *R, mv_t *X, int xs, int len, mv_t *P, mv_t
 /* GCGE_Orthonormalization, src/gcge_orthogonal.c:112-305: vector-by-vector
  * B-orthonormalisation with re-orthogonalisation; the column (MGS) form is used when
  * 0 < sum_res < criterion_tol, the block (CGS) form otherwise. Returns the new end. */
-static int orth_plain(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int orth_plain(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
-    int n = V->n;
     double *d = g->sub_dtmp;
     double vin = 0.0, vout = 0.0, ratio;
-    double *t0 = g->V_tmp.c[0], *t1 = g->V_tmp.c[1];
+    void *t0 = g->V_tmp.c[0], *t1 = g->V_tmp.c[1];
     for (int cur = start; cur < end; ++cur) {
         int reorth = 0;
         if (g->sum_res > 0.0 && g->sum_res < g->criterion_tol) {
-            double *vc = V->c[cur];
-            if (!B) vout = sqrt(vdot(n, vc, vc));
-            else { csr_mv(B, vc, t1); vout = sqrt(vdot(n, vc, t1)); }
+            void *vc = V->c[cur];
+            if (!B) vout = sqrt(vdot(vc, vc));
+            else { csr_mv(B, vc, t1); vout = sqrt(vdot(vc, t1)); }
             do {
                 for (int j = 0; j < cur; ++j) {
                     double ipv;
-                    if (!B) ipv = vdot(n, vc, V->c[j]);
-                    else { csr_mv(B, vc, t1); ipv = vdot(n, V->c[j], t1); }
-                    vaxpby(n, -ipv, V->c[j], 1.0, vc);
+                    if (!B) ipv = vdot(vc, V->c[j]);
+                    else { csr_mv(B, vc, t1); ipv = vdot(V->c[j], t1); }
+                    vaxpby(-ipv, V->c[j], 1.0, vc);
                 }
                 vin = vout;
                 double nv;
-                if (!B) nv = vdot(n, vc, vc);
-                else { csr_mv(B, vc, t1); nv = vdot(n, vc, t1); }
+                if (!B) nv = vdot(vc, vc);
+                else { csr_mv(B, vc, t1); nv = vdot(vc, t1); }
                 vout = sqrt(nv);
                 ratio = vout / vin;
                 /* the reference never advances its counter on this path
@@ -267,14 +423,14 @@ static int orth_plain(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
             } while (ratio < g->reorth_tol && reorth < g->max_reorth_time && vout > g->orth_zero_tol);
         } else {
             do {
-                if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, t0);
+                if (!B) vaxpby(1.0, V->c[cur], 0.0, t0);
                 else csr_mv(B, V->c[cur], t0);
                 int s[2] = {0, 0}, e[2] = {cur + 1, 1};
                 mv_inner(V, &g->V_tmp, d, 0, s, e, cur + 1);
                 if (cur != 0) {
                     int s2[2] = {0, 0}, e2[2] = {cur, 1};
                     mv_lincomb(V, &g->V_tmp, s2, e2, d, cur);
-                    vaxpby(n, -1.0, t0, 1.0, V->c[cur]);
+                    vaxpby(-1.0, t0, 1.0, V->c[cur]);
                 }
                 vin = sqrt(d[cur]);
                 d[cur] = d[cur] - arr_dot(d, d, cur);
@@ -284,7 +440,7 @@ static int orth_plain(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
             } while (ratio < g->reorth_tol && reorth < g->max_reorth_time && vout > g->orth_zero_tol);
         }
         if (vout > g->orth_zero_tol) {
-            vaxpby(n, 0.0, V->c[cur], 1.0 / vout, V->c[cur]);
+            vaxpby(0.0, V->c[cur], 1.0 / vout, V->c[cur]);
         } else {
             int s[2] = {cur, end - 1}, e[2] = {cur + 1, end};
             mv_swap(V, V, s, e);
@@ -300,16 +456,16 @@ static int orth_plain(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
  * W[:, start:end) projected against each of X and P in turn (classical per
  * vector, V^T evec / V^T V_tmp), and W itself by modified Gram-Schmidt with its
  * B-norm; a column of norm <= orth_zero_tol is swapped to the end and dropped. */
-static int bgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int bgs_orth(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
-    const int n = V->n, nev = g->nev, dim_xp = g->dim_xp;
+    const int nev = g->nev, dim_xp = g->dim_xp;
     double *d = g->sub_dtmp;
     for (int j = 0; j < nev; ++j) {
-        if (!B) vaxpby(n, 1.0, V->c[j], 0.0, g->evec.c[j]);
+        if (!B) vaxpby(1.0, V->c[j], 0.0, g->evec.c[j]);
         else csr_mv(B, V->c[j], g->evec.c[j]);
     }
     for (int j = nev; j < dim_xp; ++j) {
-        if (!B) vaxpby(n, 1.0, V->c[j], 0.0, g->V_tmp.c[j - nev]);
+        if (!B) vaxpby(1.0, V->c[j], 0.0, g->V_tmp.c[j - nev]);
         else csr_mv(B, V->c[j], g->V_tmp.c[j - nev]);
     }
     for (int i = 0; i < 2; ++i) {
@@ -317,23 +473,23 @@ static int bgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
         for (int cur = 0; cur < nev; ++cur) {
             int s[2] = {start, cur}, e[2] = {end, cur + 1};
             mv_inner(V, &g->evec, d, 0, s, e, wl);
-            for (int j = start; j < end; ++j) vaxpby(n, -d[j - start], V->c[cur], 1.0, V->c[j]);
+            for (int j = start; j < end; ++j) vaxpby(-d[j - start], V->c[cur], 1.0, V->c[j]);
         }
         for (int cur = nev; cur < dim_xp; ++cur) {
             int s[2] = {start, cur - nev}, e[2] = {end, cur + 1 - nev};
             mv_inner(V, &g->V_tmp, d, 0, s, e, wl);
-            for (int j = start; j < end; ++j) vaxpby(n, -d[j - start], V->c[cur], 1.0, V->c[j]);
+            for (int j = start; j < end; ++j) vaxpby(-d[j - start], V->c[cur], 1.0, V->c[j]);
         }
         for (int cur = start; cur < end; cur++) {
-            if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, g->CG_p.c[0]);
+            if (!B) vaxpby(1.0, V->c[cur], 0.0, g->CG_p.c[0]);
             else csr_mv(B, V->c[cur], g->CG_p.c[0]);
             int s[2] = {cur, 0}, e[2] = {end, 1};
             wl = end - cur;
             mv_inner(V, &g->CG_p, d, 0, s, e, wl);
             const double nv = sqrt(d[0]);
             if (nv > g->orth_zero_tol) {
-                vaxpby(n, 0.0, V->c[cur], 1.0 / nv, V->c[cur]);
-                for (int j = cur + 1; j < end; ++j) vaxpby(n, -d[j - cur] / nv, V->c[cur], 1.0, V->c[j]);
+                vaxpby(0.0, V->c[cur], 1.0 / nv, V->c[cur]);
+                for (int j = cur + 1; j < end; ++j) vaxpby(-d[j - cur] / nv, V->c[cur], 1.0, V->c[j]);
             } else {
                 int s2[2] = {cur, end - 1}, e2[2] = {cur + 1, end};
                 mv_swap(V, V, s2, e2);
@@ -351,9 +507,9 @@ static int bgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
  * eigenvectors of eigenvalues >= orth_zero_tol scaled by theta^-1/2 (everything up
  * to the last smaller one dropped), W <- W Q (the linear combination's stride and
  * offset use the reduced count, as the reference does), swapped into V. */
-static int cbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int cbgs_orth(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
-    const int n = V->n, w0 = end - start;
+    const int w0 = end - start;
     double *d = g->sub_dtmp, *tmp_evec = g->sub_evec, *tmp_eval = tmp_evec + (size_t)w0 * w0;
     double *dwork = d + (size_t)w0 * w0;
     int *iwork = g->sub_itmp, *ifail = g->sub_itmp + 5 * w0;
@@ -370,7 +526,7 @@ static int cbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
         mv_axpby(-1.0, &g->V_tmp, 1.0, V, s2, e2);
     }
     for (int j = 0; j < wl; ++j) {
-        if (!B) vaxpby(n, 1.0, V->c[j + start], 0.0, g->V_tmp.c[j]);
+        if (!B) vaxpby(1.0, V->c[j + start], 0.0, g->V_tmp.c[j]);
         else csr_mv(B, V->c[j + start], g->V_tmp.c[j]);
     }
     {
@@ -387,7 +543,7 @@ static int cbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
     double vl = 0.0, vu = 0.0, abstol = 0.0;
     int il = 1, iu = wl, m = iu - il + 1, lwork = 8 * w0, info = 0, nn = wl;
     char V_ = 'V', I_ = 'I', U_ = 'U';
-    scipy_dsyevx_(&V_, &I_, &U_, &nn, d, &nn, &vl, &vu, &il, &iu, &abstol, &m, tmp_eval, tmp_evec, &nn, dwork, &lwork,
+    dsyevx(&V_, &I_, &U_, &nn, d, &nn, &vl, &vu, &il, &iu, &abstol, &m, tmp_eval, tmp_evec, &nn, dwork, &lwork,
                   iwork, ifail, &info);
     int nz = 0;
     for (int j = 0; j < wl; ++j) {
@@ -411,7 +567,7 @@ static int cbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
  * projection onto V[:, dim_xp:start), repeated while the summed squares of the
  * first (start - dim_xp) * w entries of the Gram buffer exceed scbgs_reorth_tol
  * (the Gram is stored with leading dimension start, as the reference does) */
-static void scb_minus(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static void scb_minus(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
     const int wl = end - start, dim_xp = g->dim_xp, length = (start - dim_xp) * wl;
     double *d = g->sub_dtmp, vi = 1.0;
@@ -435,20 +591,19 @@ static void scb_minus(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
 
 /* GCGE_SCBOrth_Self, src/gcge_orthogonal.c:1196-1281: modified Gram-Schmidt in the
  * B inner product within W[:, start:end), scbgs_wself_max_reorth_time (1) times */
-static int scb_self(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int scb_self(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
-    const int n = V->n;
     double *d = g->sub_dtmp;
     for (int it = 0; it < 1; ++it) {
         for (int cur = start; cur < end; cur++) {
-            if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, g->CG_p.c[0]);
+            if (!B) vaxpby(1.0, V->c[cur], 0.0, g->CG_p.c[0]);
             else csr_mv(B, V->c[cur], g->CG_p.c[0]);
             int s[2] = {cur, 0}, e[2] = {end, 1};
             mv_inner(V, &g->CG_p, d, 0, s, e, end - cur);
             const double nv = sqrt(d[0]);
             if (nv > g->orth_zero_tol) {
-                vaxpby(n, 0.0, V->c[cur], 1.0 / nv, V->c[cur]);
-                for (int j = cur + 1; j < end; ++j) vaxpby(n, -d[j - cur] / nv, V->c[cur], 1.0, V->c[j]);
+                vaxpby(0.0, V->c[cur], 1.0 / nv, V->c[cur]);
+                for (int j = cur + 1; j < end; ++j) vaxpby(-d[j - cur] / nv, V->c[cur], 1.0, V->c[j]);
             } else {
                 int s2[2] = {cur, end - 1}, e2[2] = {cur + 1, end};
                 mv_swap(V, V, s2, e2);
@@ -466,7 +621,7 @@ static int scb_self(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
  * w_orth_block_size = max(block_size / 5, 1) (src/gcge_para.c:373-376): each block
  * projected against the W columns before it and orthonormalised by itself; columns
  * a block drops are swapped behind the remaining ones */
-static int scbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int scbgs_orth(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
     const int w0 = end - start, length = start * w0;
     double *d = g->sub_dtmp, vi = 1.0;
@@ -509,7 +664,7 @@ static int scbgs_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
 
 /* GCGE_SubOrthonormalization, src/gcge_orthogonal.c:1880-1929:
  * V2 -= V1 (V1^T B V2), Gram left in sub_dtmp (len1 x len2, ld len1). */
-static void sub_orth(gcge_t *g, mv_t *V, const int *s, const int *e, const csr_t *B)
+static void sub_orth(gcge_t *g, mv_t *V, const int *s, const int *e, void *B)
 {
     int len1 = e[0] - s[0], len2 = e[1] - s[1];
     int ms[2] = {s[1], 0}, me[2] = {e[1], len2};
@@ -523,20 +678,20 @@ static void sub_orth(gcge_t *g, mv_t *V, const int *s, const int *e, const csr_t
 }
 
 /* GCGE_SubOrthonormalizationSelfBGS, src/gcge_orthogonal.c:2035-2115 */
-static int self_bgs(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int self_bgs(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
-    int n = V->n;
-    double *d = g->sub_dtmp, *t0 = g->V_tmp.c[0];
+    double *d = g->sub_dtmp;
+    void *t0 = g->V_tmp.c[0];
     for (int cur = start; cur < end; ++cur) {
-        if (!B) vaxpby(n, 1.0, V->c[cur], 0.0, t0);
+        if (!B) vaxpby(1.0, V->c[cur], 0.0, t0);
         else csr_mv(B, V->c[cur], t0);
         int s[2] = {cur, 0}, e[2] = {end, 1};
         mv_inner(V, &g->V_tmp, d, 0, s, e, end - cur);
         double nrm = sqrt(d[0]);
         if (nrm > g->orth_zero_tol) {
-            vaxpby(n, 0.0, V->c[cur], 1.0 / nrm, V->c[cur]);
+            vaxpby(0.0, V->c[cur], 1.0 / nrm, V->c[cur]);
             for (int j = cur + 1; j < end; ++j)
-                vaxpby(n, -d[j - cur] / nrm, V->c[cur], 1.0, V->c[j]);
+                vaxpby(-d[j - cur] / nrm, V->c[cur], 1.0, V->c[j]);
         } else {
             int s2[2] = {cur, end - 1}, e2[2] = {cur + 1, end};
             mv_swap(V, V, s2, e2);
@@ -549,7 +704,7 @@ static int self_bgs(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
 
 /* GCGE_MultiOrthonormalization, src/gcge_orthogonal.c:1945-2033: recursive
  * bisection; leaves (length <= max_direct_orth_length = 1) go to SelfBGS. */
-static int multi_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int multi_orth(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
     int length = end - start;
     int l1 = length / 2, l2 = length - l1, mid = start + l1;
@@ -578,7 +733,7 @@ static int multi_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
 }
 
 /* GCGE_StableMultiOrthonormalization, src/gcge_orthogonal.c:1833-1877 */
-static int stable_multi_orth(gcge_t *g, mv_t *V, int start, int end, const csr_t *B)
+static int stable_multi_orth(gcge_t *g, mv_t *V, int start, int end, void *B)
 {
     double value_inner = 1.0;
     int iter = 0;
@@ -640,7 +795,7 @@ static int stable_multi_orth_sub(gcge_t *g, double *V, int ldV, int nrows, int s
 
 /* ----------------------------------------------------- Rayleigh-Ritz (a16/a17) */
 /* GCGE_ComputeSubspaceMatrixVTAW, src/gcge_rayleighritz.c:35-81 */
-static void rr_vtaw(gcge_t *g, const csr_t *A, int start_W, int end_V, double *sub)
+static void rr_vtaw(gcge_t *g, void *A, int start_W, int end_V, double *sub)
 {
     int w_len = end_V - start_W, xp_len = end_V - w_len;
     int s[2] = {start_W, 0}, e[2] = {end_V, w_len};
@@ -651,7 +806,7 @@ static void rr_vtaw(gcge_t *g, const csr_t *A, int start_W, int end_V, double *s
 }
 
 /* GCGE_ComputeSubspaceMatrix, src/gcge_rayleighritz.c:113-200 (structured form) */
-static void rr_matrix(gcge_t *g, const csr_t *A)
+static void rr_matrix(gcge_t *g, void *A)
 {
     int dim_xp = g->dim_xp, ldm = g->dim_xpw;
     if (dim_xp != 0) {
@@ -697,7 +852,7 @@ static int rr_eig(gcge_t *g)
     il -= start;
     iu -= start;
     char V = 'V', I = 'I', U = 'U';
-    scipy_dsyevx_(&V, &I, &U, &nrows, tmp + (size_t)start * ncols + start, &ncols, &vl, &vu, &il, &iu, &abstol, &m,
+    dsyevx(&V, &I, &U, &nrows, tmp + (size_t)start * ncols + start, &ncols, &vl, &vu, &il, &iu, &abstol, &m,
                   g->eval + start, g->sub_evec + (size_t)start * ldm + start, &ldm, work, &lwork, iwork, ifail,
                   &info);
     return info;
@@ -713,21 +868,21 @@ static void compute_x(gcge_t *g, int size_x, int size_v)
 }
 
 /* GCGE_ComputeW, src/gcge_xpw.c:118-217 (built-in block CG, no external solver) */
-static void compute_w(gcge_t *g, const csr_t *A, const csr_t *B)
+static void compute_w(gcge_t *g, void *A, void *B)
 {
-    int n = A->n, ws = g->dim_xp, wl = g->unconv_bs;
+    int ws = g->dim_xp, wl = g->unconv_bs;
     for (int idx = 0; idx < wl; ++idx) {
-        double *rhs = g->V_tmp.c[idx];
+        void *rhs = g->V_tmp.c[idx];
         int xi = g->unlock[idx];
-        double *x = g->V.c[xi], *w = g->V.c[ws + idx];
-        if (!B) vaxpby(n, 1.0, x, 0.0, rhs);
+        void *x = g->V.c[xi], *w = g->V.c[ws + idx];
+        if (!B) vaxpby(1.0, x, 0.0, rhs);
         else csr_mv(B, x, rhs);
         double lam = g->eval[xi];
         if (fabs(lam) <= 1.0) {
-            vaxpby(n, 0.0, rhs, lam, rhs);
-            vaxpby(n, 1.0, x, 0.0, w);
+            vaxpby(0.0, rhs, lam, rhs);
+            vaxpby(1.0, x, 0.0, w);
         } else {
-            vaxpby(n, 1.0 / lam, x, 0.0, w);
+            vaxpby(1.0 / lam, x, 0.0, w);
         }
     }
     bcg(A, &g->V_tmp, &g->V, ws, wl, &g->CG_p, &g->evec, g->sub_dtmp, g->sub_itmp,
@@ -760,24 +915,25 @@ static void compute_p(gcge_t *g)
 
 /* ------------------------------------------------------ convergence (a18/a19) */
 /* GCGE_CheckConvergence, src/gcge_eigsol.c:559-686, plus the "BR" criterion */
-static void check_conv(gcge_t *g, const csr_t *A, const csr_t *B)
+static void check_conv(gcge_t *g, void *A, void *B)
 {
-    int n = A->n, unconv = 0, max_conv_idx = 0, num_unlock = g->num_unlock;
+    int unconv = 0, max_conv_idx = 0, num_unlock = g->num_unlock;
     double max_res = 0.0, min_res = 0.0, sum_res = 0.0;
-    double *t1 = g->V_tmp.c[0], *t2 = g->V_tmp.c[1];
+    void *t1 = g->V_tmp.c[0], *t2 = g->V_tmp.c[1];
     for (int j = 0; j < num_unlock; ++j) {
         int i = g->unlock[j];
-        double *ev = g->evec.c[i], lam = g->eval[i], bxn = 0.0;
+        void *ev = g->evec.c[i];
+        double lam = g->eval[i], bxn = 0.0;
         csr_mv(A, ev, t1);
-        if (!B) { vaxpby(n, -lam, ev, 1.0, t1); }
-        else { csr_mv(B, ev, t2); vaxpby(n, -lam, t2, 1.0, t1); }
-        double rn = sqrt(vdot(n, t1, t1));
-        double en = sqrt(vdot(n, ev, ev));
+        if (!B) { vaxpby(-lam, ev, 1.0, t1); }
+        else { csr_mv(B, ev, t2); vaxpby(-lam, t2, 1.0, t1); }
+        double rn = sqrt(vdot(t1, t1));
+        double en = sqrt(vdot(ev, ev));
         double r;
         if (strcmp(g->conv_type, "R") == 0) r = rn / en / (1.0 > fabs(lam) ? 1.0 : fabs(lam));
         else if (strcmp(g->conv_type, "O") == 0) r = rn / en / (g->conv_omega_norm + fabs(lam));
         else if (strcmp(g->conv_type, "BR") == 0) {
-            bxn = B ? sqrt(vdot(n, t2, t2)) : en;
+            bxn = B ? sqrt(vdot(t2, t2)) : en;
             r = rn / (fabs(lam) * bxn);
         } else r = rn / en;
         g->res[i] = r;
@@ -814,9 +970,11 @@ static int check_multiplicity(int nev, int end, const double *eval)
     return t;
 }
 
-/* CSR_SetDirichletBoundary, app/csr/gcge_app_csr.c:130-183 */
-static void dirichlet_zero(gcge_t *g, const csr_t *A, const csr_t *B)
+/* CSR_SetDirichletBoundary, app/csr/gcge_app_csr.c:130-183: rows where B has no
+ * nonzero and A a single one are Dirichlet rows; the vectors are zeroed there */
+static void h_dirichlet(void **vecs, int nev, void *Av, void *Bv)
 {
+    const csr_t *A = (const csr_t *)Av, *B = (const csr_t *)Bv;
     if (!A || !B) return;
     for (int i = 0; i < A->n; ++i) {
         int zero_b = 1;
@@ -827,8 +985,15 @@ static void dirichlet_zero(gcge_t *g, const csr_t *A, const csr_t *B)
         for (int j = A->rp[i]; j < A->rp[i + 1]; ++j)
             if (fabs(A->v[j]) > 1e-20) cnt++;
         if (cnt == 1)
-            for (int k = 0; k < g->nev; ++k) g->evec.c[k][i] = 0.0;
+            for (int k = 0; k < nev; ++k) hcol(vecs[k])[i] = 0.0;
     }
+}
+
+/* ops->SetDirichletBoundary(evec, nev, A, B), src/gcge_eigsol.c:176-179 */
+static void dirichlet_zero(gcge_t *g, void *A, void *B)
+{
+    if (!A || !B) return;
+    T->SetDirichletBoundary(g->evec.c, g->nev, A, B);
 }
 
 /* ------------------------------------------------------------------ solve */
@@ -842,11 +1007,19 @@ void gcge_oracle_default_params(gcge_oracle_params *p)
     p->init_rng = 0; p->seed = 1;
 }
 
+/* ops->MultiVecSetRandomValue(evec, start, count), src/gcge_eigsol.c:131-134: on
+ * the host table libc rand() after srand(seed) (CSR_VecSetRandomValue,
+ * app/csr/gcge_app_csr.c:284-294) or the counter hash; a caller's table draws
+ * from its own generator */
 static void random_columns(gcge_t *g, const gcge_oracle_params *p, int from, int count)
 {
+    if (!g_host) {
+        T->MultiVecSetRandomValue(g->evec.c, from, count, T);
+        return;
+    }
     int n = g->evec.n;
     for (int j = from; j < from + count; ++j) {
-        double *c = g->evec.c[j];
+        double *c = hcol(g->evec.c[j]);
         if (p->init_rng == 0) {
             for (int i = 0; i < n; ++i) c[i] = ((double)rand()) / ((double)RAND_MAX + 1);
         } else {
@@ -856,15 +1029,14 @@ static void random_columns(gcge_t *g, const gcge_oracle_params *p, int from, int
     }
 }
 
-int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v,
-                      const int *B_rp, const int *B_ci, const double *B_v,
-                      const gcge_oracle_params *p, double *eval_out, double *evec_out,
-                      gcge_oracle_stats *st)
+/* GCGE_Solve, src/gcge_eigsol.c:65-542, over the current table. evec is the
+ * solver's eigenvector multivector (nev columns; the initial vectors when
+ * given_init_evec = 1), eval_out[nev] the eigenvalues. */
+static int solve_core(void *A, void *B, int n, const gcge_oracle_params *p, double *eval_out, mv_t *evec,
+                      double *host_evec_out, gcge_oracle_stats *st)
 {
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
-    csr_t Am = {n, A_rp, A_ci, A_v}, Bm = {n, B_rp, B_ci, B_v};
-    const csr_t *A = &Am, *B = B_rp ? &Bm : NULL;
     gcge_t G, *g = &G;
     memset(g, 0, sizeof(G));
     g->A = A; g->B = B;
@@ -891,10 +1063,10 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
     int max_dim_x = mtmp > nev + 3 ? mtmp : nev + 3;
     int bs = g->block_size;
     int V_size = max_dim_x + 2 * bs, Vt_size = max_dim_x - nev + bs, max_dim_xpw = V_size;
-    mv_alloc(&g->V, n, V_size);
-    mv_alloc(&g->V_tmp, n, Vt_size);
-    mv_alloc(&g->CG_p, n, bs);
-    mv_alloc(&g->evec, n, nev);
+    mv_alloc(&g->V, A, n, V_size);
+    mv_alloc(&g->V_tmp, A, n, Vt_size);
+    mv_alloc(&g->CG_p, A, n, bs);
+    g->evec = *evec;
     g->max_dim_x = max_dim_x; g->dim_x = nev; g->dim_xp = 0; g->dim_xpw = nev;
     g->unconv_bs = nev < bs ? nev : bs;
     g->eval = (double *)calloc(max_dim_xpw, sizeof(double));
@@ -917,13 +1089,13 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
             if (strcmp(g->conv_type, "O") == 0 && num_init == 0) {
                 double omega = 0.0, aomega = 0.0;
                 for (int i = 0; i < nev; ++i) {
-                    double nv = vdot(n, g->evec.c[i], g->evec.c[i]);
-                    vaxpby(n, 0.0, g->evec.c[i], 1.0 / sqrt(nv), g->evec.c[i]);
+                    double nv = vdot(g->evec.c[i], g->evec.c[i]);
+                    vaxpby(0.0, g->evec.c[i], 1.0 / sqrt(nv), g->evec.c[i]);
                 }
-                for (int i = 0; i < nev; ++i) omega += vdot(n, g->evec.c[i], g->evec.c[i]);
+                for (int i = 0; i < nev; ++i) omega += vdot(g->evec.c[i], g->evec.c[i]);
                 int s[2] = {0, 0}, e[2] = {nev, nev};
                 mv_matdot(A, &g->evec, &g->V, s, e);
-                for (int i = 0; i < nev; ++i) aomega += vdot(n, g->V.c[i], g->V.c[i]);
+                for (int i = 0; i < nev; ++i) aomega += vdot(g->V.c[i], g->V.c[i]);
                 g->conv_omega_norm = sqrt(aomega / omega);
             }
             if (g->dirichlet) dirichlet_zero(g, A, B);
@@ -933,7 +1105,6 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
             if (++guard > 100) { status = 2; break; }
         } while (num_init < nev);
     } else {
-        for (int j = 0; j < nev; ++j) memcpy(g->evec.c[j], evec_out + (size_t)j * n, sizeof(double) * n);
         g->dim_x = orth_plain(g, &g->evec, 0, nev, B);
     }
     {
@@ -997,7 +1168,10 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
         mv_axpby(1.0, &g->V, 0.0, &g->evec, s, e);
     }
     memcpy(eval_out, g->eval, sizeof(double) * nev);
-    for (int j = 0; j < nev; ++j) memcpy(evec_out + (size_t)j * n, g->evec.c[j], sizeof(double) * n);
+    /* host table: column j of the result is the handle in position j (swaps
+     * exchange handles, so it may live in the workspace freed below) */
+    if (g_host && host_evec_out)
+        for (int j = 0; j < nev; ++j) memcpy(host_evec_out + (size_t)j * n, hcol(g->evec.c[j]), sizeof(double) * n);
     clock_gettime(CLOCK_MONOTONIC, &t1);
     if (st) {
         st->num_iter = g->num_iter; st->num_unlock = g->num_unlock;
@@ -1005,9 +1179,45 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
         st->wall_s = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
         st->status = status;
     }
-    mv_free(&g->V); mv_free(&g->V_tmp); mv_free(&g->CG_p); mv_free(&g->evec);
+    mv_free(&g->V); mv_free(&g->V_tmp); mv_free(&g->CG_p);
     free(g->eval); free(g->sub_dtmp); free(g->sub_itmp); free(g->sub_evec); free(g->sub_mat);
     free(g->unlock); free(g->res);
+    return status;
+}
+
+int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v,
+                      const int *B_rp, const int *B_ci, const double *B_v,
+                      const gcge_oracle_params *p, double *eval_out, double *evec_out,
+                      gcge_oracle_stats *st)
+{
+    use_host_table();
+    csr_t Am = {n, A_rp, A_ci, A_v}, Bm = {n, B_rp, B_ci, B_v};
+    mv_t ev;
+    h_mv_make(&ev, n, p->nev, NULL);
+    if (p->given_init_evec)
+        for (int j = 0; j < p->nev; ++j) memcpy(hcol(ev.c[j]), evec_out + (size_t)j * n, sizeof(double) * n);
+    int status = solve_core(&Am, B_rp ? &Bm : NULL, n, p, eval_out, &ev, evec_out, st);
+    h_mv_free(&ev);
+    return status;
+}
+
+int gcge_oracle_solve_table(void *ops_table, void *A, void *B, int n, const gcge_oracle_params *p, double *eval_out,
+                            void **evec, gcge_oracle_stats *st)
+{
+    ops_t *ops = (ops_t *)ops_table;
+    if (!ops || !A || !evec || n <= 0 || p->nev <= 0) return 1;
+    /* the members GCGE_OPS_Setup requires (src/gcge_ops.c:473-520) and the block
+     * members this restatement calls */
+    if (!ops->MatDotVec || !ops->VecAxpby || !ops->VecInnerProd || !ops->MatDotMultiVec || !ops->MultiVecAxpby ||
+        !ops->MultiVecLinearComb || !ops->MultiVecInnerProd || !ops->MultiVecSwap || !ops->MultiVecCreateByMat ||
+        !ops->MultiVecDestroy || !ops->MultiVecSetRandomValue || !ops->DenseMatEigenSolver ||
+        (p->dirichlet_boundary && !ops->SetDirichletBoundary))
+        return 1;
+    T = ops;
+    g_host = 0;
+    mv_t ev = {n, p->nev, evec, NULL, NULL};
+    int status = solve_core(A, B, n, p, eval_out, &ev, NULL, st);
+    use_host_table();
     return status;
 }
 
@@ -1015,70 +1225,78 @@ int gcge_oracle_solve(int n, const int *A_rp, const int *A_ci, const double *A_v
 void gcge_oracle_csr_matvec(int n, const int *rp, const int *ci, const double *v,
                             const double *x, double *y)
 {
+    use_host_table();
     csr_t A = {n, rp, ci, v};
-    csr_mv(&A, x, y);
+    hvec_t xv = {n, (double *)x}, yv = {n, y};
+    csr_mv(&A, &xv, &yv);
 }
 
 void gcge_oracle_csr_matmultivec(int n, int k, const int *rp, const int *ci, const double *v,
                                  const double *X, double *Y)
 {
+    use_host_table();
     csr_t A = {n, rp, ci, v};
-    for (int j = 0; j < k; ++j) csr_mv(&A, X + (size_t)j * n, Y + (size_t)j * n);
+    mv_t x, y;
+    h_mv_make(&x, n, k, (double *)X);
+    h_mv_make(&y, n, k, Y);
+    int s[2] = {0, 0}, e[2] = {k, k};
+    mv_matdot(&A, &x, &y, s, e);
+    h_mv_free(&x); h_mv_free(&y);
 }
 
 void gcge_oracle_vec_axpby(int n, double a, const double *x, double b, double *y)
 {
-    vaxpby(n, a, x, b, y);
-}
-
-static void wrap_cols(mv_t *m, int n, int k, double *base)
-{
-    m->n = n; m->k = k; m->store = NULL;
-    m->c = (double **)malloc(sizeof(double *) * (k > 0 ? k : 1));
-    for (int j = 0; j < k; ++j) m->c[j] = base + (size_t)j * n;
+    use_host_table();
+    hvec_t xv = {n, (double *)x}, yv = {n, y};
+    vaxpby(a, &xv, b, &yv);
 }
 
 void gcge_oracle_multivec_lincomb(int n, int nx, int ny, const double *X, double *Y,
                                   const double *coef, int lda)
 {
+    use_host_table();
     mv_t x, y;
-    wrap_cols(&x, n, nx, (double *)X);
-    wrap_cols(&y, n, ny, Y);
+    h_mv_make(&x, n, nx, (double *)X);
+    h_mv_make(&y, n, ny, Y);
     int s[2] = {0, 0}, e[2] = {nx, ny};
     mv_lincomb(&x, &y, s, e, coef, lda);
-    free(x.c); free(y.c);
+    h_mv_free(&x); h_mv_free(&y);
 }
 
 void gcge_oracle_multivec_innerprod(int n, int nv, int nw, const double *V, const double *W,
                                     double *a, int lda, int sym)
 {
+    use_host_table();
     mv_t v, w;
-    wrap_cols(&v, n, nv, (double *)V);
-    wrap_cols(&w, n, nw, (double *)W);
+    h_mv_make(&v, n, nv, (double *)V);
+    h_mv_make(&w, n, nw, (double *)W);
     int s[2] = {0, 0}, e[2] = {nv, nw};
     mv_inner(&v, &w, a, sym, s, e, lda);
-    free(v.c); free(w.c);
+    h_mv_free(&v); h_mv_free(&w);
 }
 
 void gcge_oracle_bcg(int n, int k, const int *rp, const int *ci, const double *v,
                      double *RHS, double *W, int cg_max_it, double cg_rate)
 {
+    use_host_table();
     csr_t A = {n, rp, ci, v};
     mv_t R, X, P, Wk;
-    wrap_cols(&R, n, k, RHS);
-    wrap_cols(&X, n, k, W);
-    mv_alloc(&P, n, k);
-    mv_alloc(&Wk, n, k);
+    h_mv_make(&R, n, k, RHS);
+    h_mv_make(&X, n, k, W);
+    h_mv_make(&P, n, k, NULL);
+    h_mv_make(&Wk, n, k, NULL);
     double *dtmp = (double *)calloc(6 * (size_t)(k + 1), sizeof(double));
     int *itmp = (int *)calloc(k + 1, sizeof(int));
     bcg(&A, &R, &X, 0, k, &P, &Wk, dtmp, itmp, cg_max_it, cg_rate);
-    free(dtmp); free(itmp); mv_free(&P); mv_free(&Wk); free(R.c); free(X.c);
+    free(dtmp); free(itmp);
+    h_mv_free(&P); h_mv_free(&Wk); h_mv_free(&R); h_mv_free(&X);
 }
 
 int gcge_oracle_stable_multi_orth(int n, int ncols, double *Vd, int start, int end,
                                   const int *B_rp, const int *B_ci, const double *B_v,
                                   int max_reorth_time, double orth_zero_tol, double scbgs_reorth_tol)
 {
+    use_host_table();
     csr_t Bm = {n, B_rp, B_ci, B_v};
     gcge_t G;
     memset(&G, 0, sizeof(G));
@@ -1086,18 +1304,49 @@ int gcge_oracle_stable_multi_orth(int n, int ncols, double *Vd, int start, int e
     G.orth_zero_tol = orth_zero_tol + DBL_EPSILON;
     G.scbgs_reorth_tol = scbgs_reorth_tol + DBL_EPSILON;
     mv_t V;
-    wrap_cols(&V, n, ncols, Vd);
+    h_mv_make(&V, n, ncols, Vd);
     int width = end - start > 1 ? end - start : 1;
-    mv_alloc(&G.V_tmp, n, width);
+    h_mv_make(&G.V_tmp, n, width, NULL);
     G.sub_dtmp = (double *)calloc((size_t)(ncols + 1) * (ncols + 1) + 64, sizeof(double));
-    /* the column pointers may be permuted by zero-vector swaps: copy back in order */
+    /* the column handles may be permuted by zero-vector swaps: copy back in order */
     int new_end = stable_multi_orth(&G, &V, start, end, B_rp ? &Bm : NULL);
     double *tmp = (double *)malloc(sizeof(double) * (size_t)n * ncols);
-    for (int j = 0; j < ncols; ++j) memcpy(tmp + (size_t)j * n, V.c[j], sizeof(double) * n);
+    for (int j = 0; j < ncols; ++j) memcpy(tmp + (size_t)j * n, hcol(V.c[j]), sizeof(double) * n);
     memcpy(Vd, tmp, sizeof(double) * (size_t)n * ncols);
     free(tmp);
-    mv_free(&G.V_tmp);
+    h_mv_free(&G.V_tmp);
     free(G.sub_dtmp);
-    free(V.c);
+    h_mv_free(&V);
     return new_end;
+}
+
+/* ------------------------------------------- table-driven solve: helpers */
+size_t gcge_oracle_table_bytes(void) { return sizeof(ops_t); }
+
+void gcge_oracle_host_table(void *table) { memcpy(table, &H_OPS, sizeof(ops_t)); }
+
+void *gcge_oracle_csr_handle(int n, const int *rp, const int *ci, const double *v)
+{
+    csr_t *A = (csr_t *)malloc(sizeof(csr_t));
+    A->n = n; A->rp = rp; A->ci = ci; A->v = v;
+    return A;
+}
+void gcge_oracle_csr_handle_free(void *A) { free(A); }
+
+int gcge_oracle_table_mv_create(void *table, void *mat, int k, void ***mv)
+{
+    ops_t *ops = (ops_t *)table;
+    *mv = NULL;
+    if (!ops || !ops->MultiVecCreateByMat || !mat || k <= 0) return 1;
+    ops->MultiVecCreateByMat(mv, k, mat, ops);
+    return *mv ? 0 : 1;
+}
+void gcge_oracle_table_mv_destroy(void *table, void ***mv, int k)
+{
+    ops_t *ops = (ops_t *)table;
+    if (ops && ops->MultiVecDestroy && mv && *mv) ops->MultiVecDestroy(mv, k, ops);
+}
+void gcge_oracle_host_mv_read(void **mv, int k, int n, double *out)
+{
+    for (int j = 0; j < k; ++j) memcpy(out + (size_t)j * n, hcol(mv[j]), sizeof(double) * n);
 }

@@ -16,6 +16,8 @@
 #ifndef GCGE_ORACLE_H
 #define GCGE_ORACLE_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -68,6 +70,34 @@ int gcge_oracle_solve(int n,
                       const int *B_rp, const int *B_ci, const double *B_v,
                       const gcge_oracle_params *p,
                       double *eval, double *evec, gcge_oracle_stats *st);
+
+/* The same GCGE_Solve restatement over a caller's GCGE_OPS table (layout
+ * GCGE_GPU_OPS_LAYOUT, include/gcge_gb300_ops.h, member for member the
+ * reference's GCGE_OPS, src/gcge_ops.h:29-215): GCGE's solver core driving
+ * another backend through the table alone. A, B (B may be NULL) are the
+ * table's matrix handles, n their order; evec is the eigenvector multivector
+ * (nev handles, made by the table's MultiVecCreateByMat, as
+ * GCGE_CSR_Solver_Init does, app/csr/gcge_app_csr.c:104-112); eval[nev] gets
+ * the eigenvalues. Every n-sized operation goes through the table; the small
+ * dense work stays on the host as the reference's defaults
+ * (src/gcge_ops.c:573-604), except DenseMatEigenSolver, taken from the table.
+ * The table's MultiVecSwap must exchange column data (as the GB300 table
+ * does) or evec may end up holding workspace handles freed at exit. The
+ * initial vectors come from the table's MultiVecSetRandomValue. Returns 0 on
+ * success, 1 when the table lacks a member the solve needs. */
+int gcge_oracle_solve_table(void *ops_table, void *A, void *B, int n, const gcge_oracle_params *p,
+                            double *eval, void **evec, gcge_oracle_stats *st);
+
+/* helpers for the table-driven solve: the table size, a copy of the host CSR
+ * table (the reference's GCGE_CSR_SetOps plus defaults), a host CSR handle,
+ * multivectors made and destroyed through a table, host columns read out */
+size_t gcge_oracle_table_bytes(void);
+void gcge_oracle_host_table(void *table);
+void *gcge_oracle_csr_handle(int n, const int *rp, const int *ci, const double *v);
+void gcge_oracle_csr_handle_free(void *A);
+int  gcge_oracle_table_mv_create(void *table, void *mat, int k, void ***mv);
+void gcge_oracle_table_mv_destroy(void *table, void ***mv, int k);
+void gcge_oracle_host_mv_read(void **mv, int k, int n, double *out);
 
 /* ---- single operations, for per-kernel parity ---- */
 

@@ -101,6 +101,47 @@ class Oracle(_Lib):
         L.gcge_oracle_stable_multi_orth.restype = C.c_int
         L.gcge_oracle_hash_uniform.argtypes = [C.c_ulonglong, C.c_ulonglong]
         L.gcge_oracle_hash_uniform.restype = C.c_double
+        VP = C.c_void_p
+        L.gcge_oracle_solve_table.argtypes = [VP, VP, VP, C.c_int, C.POINTER(Params), VP, VP, C.POINTER(Stats)]
+        L.gcge_oracle_solve_table.restype = C.c_int
+        L.gcge_oracle_table_bytes.restype = C.c_size_t
+        L.gcge_oracle_host_table.argtypes = [VP]
+        L.gcge_oracle_csr_handle.argtypes = [C.c_int, VP, VP, VP]
+        L.gcge_oracle_csr_handle.restype = VP
+        L.gcge_oracle_csr_handle_free.argtypes = [VP]
+        L.gcge_oracle_table_mv_create.argtypes = [VP, VP, C.c_int, C.POINTER(VP)]
+        L.gcge_oracle_table_mv_create.restype = C.c_int
+        L.gcge_oracle_table_mv_destroy.argtypes = [VP, C.POINTER(VP), C.c_int]
+        L.gcge_oracle_host_mv_read.argtypes = [VP, C.c_int, C.c_int, VP]
+
+    # ---- GCGE's solver core over a GCGE_OPS table (the drop-in boundary)
+    def new_table(self, host=False):
+        """A zeroed GCGE_OPS-layout table (host=True: the oracle's host CSR table)."""
+        t = C.create_string_buffer(self.lib.gcge_oracle_table_bytes())
+        if host:
+            self.lib.gcge_oracle_host_table(t)
+        return t
+
+    def table_multivec(self, table, mat, k):
+        """A k-column multivector made by the table's MultiVecCreateByMat (a void ** handle)."""
+        h = C.c_void_p()
+        if self.lib.gcge_oracle_table_mv_create(table, mat, k, C.byref(h)) != 0:
+            raise RuntimeError("MultiVecCreateByMat failed")
+        return h
+
+    def table_multivec_destroy(self, table, h, k):
+        self.lib.gcge_oracle_table_mv_destroy(table, C.byref(h), k)
+
+    def solve_table(self, table, A, B, n, params, evec):
+        """The GCGE_Solve restatement driven through `table` alone; A, B: the table's
+        matrix handles (B may be None), evec: its eigenvector multivector. Returns
+        (eval, stats)."""
+        ev = np.zeros(params.nev)
+        st = Stats()
+        rc = self.lib.gcge_oracle_solve_table(table, A, B, n, C.byref(params), _ptr(ev), evec, C.byref(st))
+        if rc != 0:
+            raise RuntimeError("solve_table returned %d" % rc)
+        return ev, st
 
     # Column-major n x k blocks are held as numpy arrays of shape (k, n) (C order).
     def matmultivec(self, A, X):
