@@ -88,8 +88,8 @@ def peaks():
 
 
 # f16 digit-pair products per FP64 multiply-add of the tensor-core contractions
-# (error-free split into 7 digits; levels 0-7 for the linear combination, 0-6 for the Gram)
-TENSOR_PAIRS = {"lincomb": 34, "gram": 28}
+# (error-free split into 7 digits; digit pairs of levels 0-7 kept by both)
+TENSOR_PAIRS = {"lincomb": 34, "gram": 34}
 
 
 class ClockSampler:
@@ -157,42 +157,40 @@ def check_solution(A, B, ev, X, exact):
     return float(r.max()), float(np.max(np.abs(ev - exact) / exact))
 
 
-def cpu_sample(workload_full_n, gpu_iters=None, threads=1, ne=32):
-    """Bounded CPU run of the oracle port (restatement of the reference CSR path, scalar C;
-    OpenBLAS limited to `threads` for the small dense calls) on the same pencil family at a
-    reduced mesh (ne = 32: n = 29,791), 50 eigenpairs, block 64, residual <= 1e-8: the solve
-    is run for 2 and for 6 outer GCG iterations; t(2) covers the set-up and first steps and
-    (t(6) - t(2)) / 4 is the time of one outer iteration. The estimate for the full workload
-    is t(2) + per-iteration time x (iterations - 2), with the iteration count the GPU solve
-    needed (else 40), scaled by the row ratio (every per-iteration cost of the path is
-    linear in n at fixed nev; the small sample stays in cache, so this under-estimates)."""
+def cpu_complete_solves(budget_s=12.0, min_solves=3, threads=1):
+    """Complete CPU solves of the oracle port (scalar C restatement of the reference
+    CSR GCGE, bit-identical to the reference build; OpenBLAS limited to `threads`
+    for the small dense calls) on the 2-D 5-point Laplacian 100 x 100 (n = 10,000,
+    B = I, 10 eigenpairs, residual ||Ax - lambda x|| / (|lambda| ||x||) <= 1e-8 for
+    every pair): solves are repeated until `budget_s` of wall time has passed (at
+    least `min_solves`), each timed from start to converged eigenpairs. Returns
+    (mean seconds per solve, number of solves, iterations, max residual)."""
     code = r"""
-import json, os, sys, time
+import json, sys, time
 sys.path.insert(0, %r); sys.path.insert(0, %r)
+import numpy as np
 import pyoracle
 from gcge_gb300 import problems as P
-A, B = P.fem_q1_cube(%d)
+A, _ = P.laplace2d(100, 100)
 o = pyoracle.Oracle()
-out = {"n": A.n}
-for it in (2, 6):
-    p = o.params(nev=50, block_size=64, ev_max_it=it, conv_type="BR", init_rng=1, seed=7)
-    t = time.time(); ev, X, st = o.solve(A, B, p); out["t%%d" %% it] = time.time() - t
-print(json.dumps(out))
-""" % (os.path.join(ROOT, "gcge-1.0_gb300"), os.path.join(ROOT, "oracle"), ne)
+ts = []
+t_all = time.time()
+while len(ts) < %d or time.time() - t_all < %f:
+    p = o.params(nev=10, conv_type="BR", ev_tol=1e-8, ev_max_it=200, init_rng=1, seed=20241203)
+    t = time.time(); ev, X, st = o.solve(A, None, p); ts.append(time.time() - t)
+As = A.to_scipy()
+r = np.linalg.norm(As @ X - X * ev[None, :], axis=0) / (np.abs(ev) * np.linalg.norm(X, axis=0))
+print(json.dumps({"t": sum(ts) / len(ts), "solves": len(ts), "iters": st.num_iter, "unconv": st.num_unlock,
+                  "maxres": float(r.max())}))
+""" % (os.path.join(ROOT, "gcge-1.0_gb300"), os.path.join(ROOT, "oracle"), min_solves, budget_s)
     env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads))
-    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=600)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
     if r.returncode != 0:
-        raise RuntimeError("cpu sample failed: " + r.stderr[-2000:])
+        raise RuntimeError("cpu solve failed: " + r.stderr[-2000:])
     d = json.loads(r.stdout.strip().splitlines()[-1])
-    per_it = max(d["t6"] - d["t2"], 0.0) / 4.0
-    iters = gpu_iters if gpu_iters else 40
-    scale_n = workload_full_n / d["n"]
-    est = (d["t2"] + per_it * max(iters - 2, 0)) * scale_n
-    sample = ("oracle port (C restatement of the reference CSR GCGE) on the Q1 cube at ne=%d (n=%d, nev=50, "
-              "block 64): 2 outer iterations %.2f s, 6 outer iterations %.2f s wall; full solve estimated as "
-              "t2 + %.3f s/iteration x (%d-2), scaled by the row ratio %.1f" %
-              (ne, d["n"], d["t2"], d["t6"], per_it, iters, scale_n))
-    return est, sample
+    if d["unconv"] != 0:
+        raise RuntimeError("cpu solve did not converge: %s" % d)
+    return d
 
 
 def roofline_from_profile(prof, hbm_peak, tensor_peak=None):
@@ -236,8 +234,74 @@ def load_traffic():
         return {}
 
 
+def sig(x, d=4):
+    """A float rounded to d significant digits (keeps the JSON line short)."""
+    if x is None or isinstance(x, (int, str)) or x != x:
+        return x
+    return float("%.*g" % (d, x))
+
+
+def br_residuals(A, B, ev, X):
+    """||Ax - lambda Bx|| / (|lambda| ||Bx||) of every pair, on the host (scipy)."""
+    As = A.to_scipy()
+    AX = As @ X
+    BX = B.to_scipy() @ X if B is not None else X
+    return np.linalg.norm(AX - BX * ev[None, :], axis=0) / (np.abs(ev) * np.linalg.norm(BX, axis=0))
+
+
+# full-size configurations solved in the default run beside the headline: name ->
+# (nev, block, host-side generator, wall seconds the pair of solves is allowed
+# before the run skips it: problem generation, the mixed and the FP64 solve,
+# residual checks)
+BIG = {
+    "c3": (100, 128, "varcoef3d 160^3 (7-point, exp of a sigma-1 Gaussian field, corr. 8 cells), B=diag U[1,2]"),
+    "c5": (200, 256, "power-law graph Laplacian + 1e-3 I, n=2e6 (degrees 4..2000, exp 2.5), B=diag U[1,2]"),
+}
+
+
+def run_big(G, name, precond, device):
+    """One mixed-precision (FP32 inner block CG, every outer product FP64) and one
+    plain FP64 solve of a full-size configuration, from the same seeded initial
+    vectors, device-timed; every residual recomputed on the host; the mixed
+    eigenvalues compared with the FP64 ones."""
+    from gcge_gb300 import problems as P
+    nev, block, desc = BIG[name]
+    t0 = time.time()
+    A, B = P.varcoef3d(nc=160) if name == "c3" else P.powerlaw_graph(n=2_000_000)
+    gen = time.time() - t0
+    ctx = G.Context(device)
+    out = {"n": A.n, "nnz": A.nnz, "nev": nev, "block": block, "precond": precond}
+    try:
+        dA, dB = ctx.matrix(A, keep_fp32=True), ctx.matrix(B)
+        X = ctx.multivec(A.n, nev)
+        res = {}
+        for prec in (1, 0):
+            p = ctx.params(nev=nev, block_size=block, ev_tol=1e-8, conv_type="BR", ev_max_it=3000,
+                           seed=20241203, precision=prec, precond=precond)
+            ev, Xh, st = ctx.solve(dA, dB, p, evec=X)
+            r = br_residuals(A, B, ev, Xh)
+            res[prec] = (ev, st.solve_ms * 1e-3, st.num_iter, float(r.max()), st.num_unlock)
+            del Xh
+        ev1, t1, it1, r1, u1 = res[1]
+        ev0, t0_, it0, r0, u0 = res[0]
+        out.update({"mixed_s": sig(t1), "fp64_s": sig(t0_), "speedup": sig(t0_ / t1), "iters": [it1, it0],
+                    "max_res": [sig(r1, 3), sig(r0, 3)], "unconverged": [u1, u0],
+                    "max_rel_ev_diff": sig(float(np.max(np.abs(ev1 - ev0) / np.abs(ev0))), 3),
+                    "gen_s": sig(gen, 3)})
+    finally:
+        ctx.close()
+    return out
+
+
+# wall seconds each full-size configuration needs in the default run (generation,
+# upload, mixed and FP64 solves, host residual checks), measured on a GB300 with
+# the plain (0) and the Jacobi-preconditioned (1) inner block CG
+BIG_ESTIMATE_S = {0: {"c3": 500, "c5": 500}, 1: {"c3": 100, "c5": 180}}
+
+
 def run_gb300(args, dist):
     import gcge_gb300 as G
+    t_run = time.time()
     rank = dist.rank
     A, B, nev, block, exact, gen_s = make_problem(args.workload)
     hbm_peak, tensor_peak, peak_kind = peaks()
@@ -250,8 +314,7 @@ def run_gb300(args, dist):
                           precision=prec, seed=20241203)
 
     def solve(prec):
-        ev, Xh, st = ctx.solve(dA, dB, params(prec), evec=X)
-        return ev, Xh, st
+        return ctx.solve(dA, dB, params(prec), evec=X)
 
     for _ in range(args.warmup):
         solve(args.precision)
@@ -279,7 +342,6 @@ def run_gb300(args, dist):
     mixed_s = dist.max(sum(times) / len(times))
     ev, Xh, st = last
     res_mixed, err_mixed = check_solution(A, B, ev, Xh, exact)
-    phases = st.as_dict()["phase_ms"]
     # ---- plain FP64 on the same workload
     fp64_times, fp64_iters = [], []
     for i in range(args.fp64_warmup + args.fp64_steps):
@@ -289,6 +351,14 @@ def run_gb300(args, dist):
             fp64_iters.append(st64.num_iter)
     fp64_s = dist.max(sum(fp64_times) / len(fp64_times)) if fp64_times else None
     res64, err64 = check_solution(A, B, ev64, X64, exact) if fp64_times else (None, None)
+    # ---- the precision-2 form (outer products in FP32-pair arithmetic): not the headline
+    p2 = None
+    if args.precision != 2 and fp64_times:
+        solve(2)
+        ev2, X2, st2 = solve(2)
+        r2, _ = check_solution(A, B, ev2, X2, exact)
+        p2 = {"s": sig(st2.solve_ms * 1e-3), "iters": st2.num_iter, "max_res": sig(r2, 3),
+              "max_rel_ev_diff_vs_fp64": sig(float(np.max(np.abs(ev2 - ev64) / ev64)), 3)}
     # ---- end to end through the host-buffer C ABI call (uploads + solve + download timed)
     e2e = [float("nan")] if args.e2e_steps == 0 else []
     h2d = A.rowptr.nbytes + A.col.nbytes + A.val.nbytes + B.rowptr.nbytes + B.col.nbytes + B.val.nbytes
@@ -308,8 +378,9 @@ def run_gb300(args, dist):
     pj.precond = 1
     evj, Xj, stj = ctx.solve(dA, dB, pj, evec=X)
     resj, errj = check_solution(A, B, evj, Xj, exact)
-    jacobi = {"value": stj.solve_ms * 1e-3, "unit": "s", "iterations": stj.num_iter, "max_residual": resj,
-              "max_rel_eig_err": errj}
+    jacobi = {"s": sig(stj.solve_ms * 1e-3), "iters": stj.num_iter, "max_res": sig(resj, 3)}
+    del Xh, X64, Xj
+    ctx.close()
     out = None
     if rank == 0:
         rows = roofline_from_profile(prof, hbm_peak, tensor_peak)
@@ -321,75 +392,119 @@ def run_gb300(args, dist):
         cap = load_traffic().get(dom)
         traffic = (cap["measured_bytes"] / cap["algorithmic_bytes"] * per_launch_alg
                    if isinstance(cap, dict) else cap)
-        spmm32 = rows.get("spmm_fp32")
+        # the full per-class table goes to stderr; the JSON line keeps share and fraction
+        print(json.dumps({"kernels": rows}), file=sys.stderr)
+        kern = {c: [sig(v["share"], 3), sig(v["frac"], 3) if v["frac"] is not None else None,
+                    v["bound"]] for c, v in sorted(rows.items(), key=lambda kv: -kv[1]["ms"])}
+        # ---- the reference's own CPU-runnable configuration, complete solves on both sides:
+        # 2-D Laplacian 100 x 100, nev 10 (same parameters, same BR criterion)
+        c1 = None
         cpu = None
         if not args.no_cpu_baseline:
-            est, sample = cpu_sample(A.n, gpu_iters=int(round(statistics.mean(iters))), threads=1)
-            cpu = {"value": est, "unit": "s", "cores": 1, "kind": "port", "sample": sample}
+            from gcge_gb300 import problems as P
+            L, _ = P.laplace2d(100, 100)
+            with G.Context(dist.local) as c:
+                dL = c.matrix(L, keep_fp32=True)
+                tg = []
+                for k in range(8):
+                    pl = c.params(nev=10, conv_type="BR", ev_tol=1e-8, ev_max_it=200, seed=20241203,
+                                  precision=args.precision)
+                    evl, Xl, stl = c.solve(dL, None, pl)
+                    if k >= 3:
+                        tg.append(stl.solve_ms * 1e-3)
+            rl = br_residuals(L, None, evl, Xl)
+            dcpu = cpu_complete_solves()
+            cpu = {"value": sig(dcpu["t"]), "unit": "s", "cores": 1, "kind": "port",
+                   "sample": "%d complete solves of the oracle port (reference CSR GCGE restated, bit-identical "
+                             "to the reference build) on the 2-D Laplacian 100x100, n=10000, nev=10, BR<=1e-8, "
+                             "%d iterations; not the headline workload: one complete solve of that takes about "
+                             "20 min on one core" % (dcpu["solves"], dcpu["iters"])}
+            c1 = {"gpu_s": sig(sum(tg) / len(tg)), "cpu_s": sig(dcpu["t"]), "cpu_over_gpu": sig(dcpu["t"] / (
+                sum(tg) / len(tg))), "iters": [stl.num_iter, dcpu["iters"]],
+                  "max_res": [sig(float(rl.max()), 3), sig(dcpu["maxres"], 3)]}
+        # ---- full-size configurations beside the headline: mixed vs FP64 on each
+        big = {}
+        for name in [c for c in args.configs.split(",") if c in BIG]:
+            spent = time.time() - t_run
+            if spent + args.big_estimate_s.get(name, 600) > args.budget_s:
+                big[name] = {"skipped": "run time budget (%.0f s spent of %.0f s)" % (spent, args.budget_s)}
+                continue
+            try:
+                big[name] = run_big(G, name, args.big_precond, dist.local)
+            except Exception as e:   # reported, not hidden: the headline stands on its own
+                big[name] = {"error": str(e)[:200]}
         out = {
             "metric": METRIC, "value": mixed_s, "unit": "s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": mixed_s * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp64 + fp32 inner block CG" + (" + fp32-pair outer SpMM" if args.precision == 2 else ""),
+            "dtype": "fp64 (outer products, Gram, Cholesky, eigensolve, residuals) + fp32 inner block CG"
+                     + (" + fp32-pair outer SpMM" if args.precision == 2 else ""),
             "data": "synthetic (exactly assembled Q1 FEM pencil, closed-form spectrum)",
             "config": {"workload": "Q1 FEM cube %d^3 elements, n=%d, nnz(A)=%d, nnz(B)=%d, nev=%d, block=%d, "
-                                   "residual ||Ax-lBx||/(|l||Bx||)<=1e-8" % (WORKLOADS[args.workload][0], A.n,
-                                                                              A.nnz, B.nnz, nev, block),
-                       "form": "mixed (precision %d)" % args.precision, "parallelism": "replicas" if dist.world > 1 else "single GPU",
+                                   "BR<=1e-8" % (WORKLOADS[args.workload][0], A.n, A.nnz, B.nnz, nev, block),
+                       "form": "mixed (precision %d)" % args.precision,
+                       "parallelism": "replicas" if dist.world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (A+B %.0f MB > 129 MB)" % (h2d / 1e6),
-                       "problem_generation_s": gen_s},
-            "fp64": {"value": fp64_s, "unit": "s", "iterations": fp64_iters, "max_residual": res64,
-                     "max_rel_eig_err": err64},
-            "speedup_mixed_vs_fp64": (fp64_s / mixed_s) if fp64_s else None,
-            "fp64_phase_ms_last_step": st64.as_dict()["phase_ms"] if fp64_times else None,
-            "mixed": {"iterations": iters, "max_residual": res_mixed, "max_rel_eig_err": err_mixed,
-                      "wall_s_timed_region": wall, "phase_ms_last_step": phases},
-            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "jacobi_inner_solve": jacobi,
+                       "why_not_c3": "the 160^3 mixed config takes ~2 min per solve; it is solved once per run "
+                                     "(key c3), not K times"},
+            "e2e": {"value": sig(e2e_s), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
-            "roofline": {"kernel": dom, "bound": d["bound"],
-                         "achieved": {"fp64": d["achieved_tflops"], "tensor": d.get("achieved_tensor_tflops"),
-                                      "fp32": d.get("achieved_fp32_tops")}
-                         .get(d["bound"], d["achieved_gbs"]), "peak": d["peak"], "unit": d["unit"], "frac": d["frac"],
-                         "peak_source": {"fp64": "FP64 FMA throughput measured on GB300 (profiles)",
-                                         "fp32": "FP32 FMA throughput measured on GB300 (profiles)",
-                                         "tensor": "MEASURED_PEAKS.json bf16_tflops_sustained (%s)" % peak_kind}
-                         .get(d["bound"], "MEASURED_PEAKS.json hbm_gbs (%s)" % peak_kind),
-                         "traffic": traffic, "alg_bytes_per_launch": per_launch_alg,
-                         "share_of_kernel_time": d["share"]},
-            "roofline_spmm_fp32": ({"bound": "hbm", "achieved": spmm32["achieved_gbs"], "peak": hbm_peak,
-                                    "unit": "GB/s", "frac": spmm32["frac"],
-                                    "traffic": load_traffic().get("spmm_fp32")} if spmm32 else None),
-            "kernels": rows,
+            "roofline": {"kernel": dom, "bound": "hbm" if d["bound"] != "tensor" else "tensor",
+                         "achieved": sig(d["achieved_gbs"]) if d["bound"] != "tensor" else sig(
+                             d["achieved_tensor_tflops"]),
+                         "peak": hbm_peak if d["bound"] != "tensor" else tensor_peak,
+                         "unit": "GB/s" if d["bound"] != "tensor" else "TFLOP/s",
+                         "frac": sig(d["achieved_gbs"] / hbm_peak if d["bound"] != "tensor" else d["frac"], 3),
+                         "traffic": sig(traffic), "alg_bytes_per_launch": sig(per_launch_alg),
+                         "peak_source": "MEASURED_PEAKS.json (%s)" % peak_kind,
+                         "pipe": ({"bound": d["bound"], "achieved": sig(d["achieved_tflops"]), "peak": d["peak"],
+                                   "unit": d["unit"], "frac": sig(d["frac"], 3)}
+                                  if d["bound"] not in ("hbm", "tensor") else None),
+                         "share": sig(d["share"], 3)},
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "kernels": kern,
+            "mixed": {"iters": iters[-1], "max_res": sig(res_mixed, 3), "max_rel_eig_err": sig(err_mixed, 3),
+                      "timed_wall_s": sig(wall)},
+            "jacobi_inner_solve": jacobi,
+            "precision2": p2,
+            "c1": c1,
+            "fp64": {"value": sig(fp64_s), "unit": "s", "iters": fp64_iters, "max_res": sig(res64, 3),
+                     "max_rel_eig_err": sig(err64, 3)},
+            "speedup_mixed_vs_fp64": sig(fp64_s / mixed_s) if fp64_s else None,
         }
-    ctx.close()
+        out.update(big)
+        out["run_wall_s"] = sig(time.time() - t_run)
     return out
 
 
 def run_reference(args, dist):
-    """The reference arm: the oracle port of the reference CSR GCGE (the compiled reference
-    is x86-only in this tree) on the host cores, same workload, metric and unit."""
+    """The reference arm. The reference CSR GCGE is single-threaded C (only its small
+    dense BLAS/LAPACK calls can use more cores); its compiled form is x86-only in this
+    tree, and its restatement (the oracle port, bit-identical to it) takes about 20
+    minutes on one core for one complete solve of the headline workload, so K
+    complete solves cannot run inside one bench run. Rather than report an estimate,
+    the line carries value null with that reason, and a measured CPU baseline on the
+    reference's own CPU-runnable configuration (complete solves, 2-D Laplacian
+    100 x 100, nev 10)."""
     if dist.rank != 0:
         return None
-    from gcge_gb300 import problems as P
     ne, nev, block = WORKLOADS[args.workload]
     n_full = (ne - 1) ** 3
-    threads = os.cpu_count() or 1
-    vals = []
-    for i in range(args.warmup + args.steps):
-        est, sample = cpu_sample(n_full, gpu_iters=None, threads=threads)
-        if i >= args.warmup:
-            vals.append(est)
-    v = statistics.mean(vals)
-    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": dist.world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+    d = cpu_complete_solves(budget_s=12.0)
+    reason = ("one complete solve of the reference CPU path (oracle port, single-threaded C like the reference) "
+              "on this workload takes ~20 min on one core, so %d complete solves do not fit one bench run; no "
+              "estimate is reported" % (args.steps + args.warmup))
+    return {"impl": "reference", "metric": METRIC, "value": None, "unit": "s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "reason": reason,
             "config": {"workload": "Q1 FEM cube %d^3 elements, n=%d, nev=%d, block=%d, BR<=1e-8"
                                    % (ne, n_full, nev, block), "form": "reference CPU path"},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
-            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": sig(d["t"]), "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "%d complete solves of the oracle port on the 2-D Laplacian 100x100 "
+                                       "(n=10000, nev=10, BR<=1e-8, %d iterations)" % (d["solves"], d["iters"])},
+            "e2e": {"value": None, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def run_kernel(args):
@@ -545,8 +660,15 @@ def main():
     ap.add_argument("--k", type=int, default=64, help="columns for --kernel spmm_a/spmm_b/bcg32")
     ap.add_argument("--nc", type=int, default=None, help="cells per edge for --kernel adjoint (512) / c3 (160)")
     ap.add_argument("--precond", type=int, default=0, help="inner block CG for --kernel c3/c5: 0 plain, 1 Jacobi")
-    ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
-                    help="mixed form of the headline solve: 1 FP32 inner block CG; 2 also FP32-pair outer products")
+    ap.add_argument("--precision", type=int, default=1, choices=[1, 2],
+                    help="mixed form of the headline solve: 1 FP32 inner block CG (every outer product FP64); "
+                         "2 also FP32-pair outer products")
+    ap.add_argument("--configs", default="c1,c3,c5",
+                    help="full-size configurations solved once each beside the headline (mixed vs FP64)")
+    ap.add_argument("--big-precond", type=int, default=0,
+                    help="inner block CG of the c3/c5 solves: 0 plain (the reference's), 1 Jacobi")
+    ap.add_argument("--budget-s", type=float, default=1500.0,
+                    help="wall seconds after which the remaining full-size configurations are skipped")
     ap.add_argument("--pair", type=int, default=0, help="--kernel spmm_a/spmm_b: 1 FP32-pair product")
     args = ap.parse_args()
     if args.nc is None:
@@ -556,6 +678,9 @@ def main():
     if args.kernel:
         run_kernel(args)
         return
+    args.big_estimate_s = BIG_ESTIMATE_S[args.big_precond]
+    if "c1" not in args.configs.split(","):
+        args.no_cpu_baseline = True
     dist = Dist()
     out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
     if out is not None and dist.rank == 0:

@@ -113,6 +113,13 @@ extern "C" int GCGE_GPU_SetTensorEmulation(gcge_gpu_ctx *ctx, int on)
     return GCGE_GPU_OK;
 }
 
+extern "C" int GCGE_GPU_TestStallTensorWait(gcge_gpu_ctx *ctx, int on)
+{
+    if (!ctx) return GCGE_GPU_ERR_ARG;
+    ctx->tc_stall = on ? 1 : 0;
+    return GCGE_GPU_OK;
+}
+
 extern "C" int GCGE_GPU_SetPairSpMM(gcge_gpu_ctx *ctx, int on)
 {
     if (!ctx) return GCGE_GPU_ERR_ARG;

@@ -62,6 +62,7 @@ struct gcge_gpu_ctx {
     void *ozbuf;               /* pre-split digit planes of small operands */
     size_t ozbuf_cap;          /* bytes */
     int *dev_err;              /* device word: set by a kernel whose bounded wait ran out */
+    int tc_stall;              /* test hook: the next tensor-core launch withholds an arrival */
     /* FP64 SpMM in FP32-pair arithmetic (1; set by the mixed solver form) or on the
      * FP64 pipe (0, default) */
     int spmm_pair;

@@ -11,9 +11,8 @@
 //    column (gb_tc05.h: oz_bias) as seven balanced base-256 digits, each exact
 //    in f16, with integer operations only;
 //  * a product x y is sum_{p,q} d_p d'_q 2^(-8(p+q)) 2^(e + f - 10); the digit
-//    pairs of levels p + q < LEVELS are kept (8 levels, 34 pairs for the linear
-//    combination; 7 levels, 28 pairs for the Gram, whose dropped terms average
-//    out over its rows);
+//    pairs of levels p + q < 8 are kept (34 pairs; the dropped ones lie below
+//    2^-57 of the scale product per term);
 //  * all pairs of one level L = p + q share one FP32 accumulator in TMEM, which
 //    stays an exact integer for up to OZ_EXACT_TERMS terms; it is drained at
 //    most every OZ_EXACT_TERMS terms into exact int64 sums (levels 0-2 and the
@@ -23,7 +22,7 @@
 //  * 16 warps, one CTA per SM; warps 0-14 split FP64 operands into f16 digit
 //    planes in shared memory (two stages of K = 32, no-swizzle K-major core
 //    matrices), lane 0 of warp 15 issues the digit-pair MMAs of a stage
-//    (M = 128, N = 64, K = 16, accumulators: 7 or 8 levels x 64 TMEM columns), and
+//    (M = 128, N = 64, K = 16, accumulators: 8 levels x 64 TMEM columns), and
 //    all 16 warps drain TMEM (warp w: lanes 32 (w % 4) .. +31, 16 columns from
 //    16 (w / 4));
 //  * hand-offs through mbarriers: full[b] (stage b written, 480 arrivals),
@@ -128,13 +127,21 @@ __device__ __forceinline__ void tc_setup(tc_hdr *h)
 // levels) instead of 34 (28), and each A plane is read from shared memory once
 // per such group instead of once per pair. The first K step of a chunk keeps
 // the pairwise order, whose first MMA into every level overwrites it.
+// stall (test hook, GCGE_GPU_TestStallTensorWait): before the first stage the
+// issuing thread waits for the first drain, an arrival that cannot come before
+// the MMAs it would issue, so that bounded wait runs out and the CTA takes the
+// timeout path (no MMA is issued; the other warps' waits run out in turn).
 template <int LEVELS, bool COPIED>
 __device__ __forceinline__ void tc_issue_stage(tc_hdr *h, uint32_t sbase, uint32_t tmem, int N, int s, int cs,
-                                               int *commits, int *err)
+                                               int *commits, int *err, int stall)
 {
     const int buf = s & 1;
     const uint32_t full = tc_smem_addr(h->bar) + 8 * buf, empty = tc_smem_addr(h->bar) + 16 + 8 * buf;
     const uint32_t drained = tc_smem_addr(h->bar) + 32, copied = tc_smem_addr(h->bar) + 40 + 8 * buf;
+    if (stall && s == 0 && !tc_mbar_wait(drained, 0, TC_WAIT_NS)) {
+        tc_fail(h, err);
+        return;
+    }
     bool ok = tc_mbar_wait(full, (s >> 1) & 1, TC_WAIT_NS);
     if (COPIED && ok) ok = tc_mbar_wait(copied, (s >> 1) & 1, TC_WAIT_NS);
     if (ok && cs == 0 && s > 0) ok = tc_mbar_wait(drained, (commits[2] - 1) & 1, TC_WAIT_NS);
@@ -277,9 +284,14 @@ __global__ void k_fill_int(int *p, int count, int v)
 
 // ---------------------------------------------------------------- Gram V^T W (tcgen05)
 #define GR_CORES_PER_WARP ((TC_ACORES + TC_BCORES + TC_SPLIT_WARPS - 1) / TC_SPLIT_WARPS)
-// Levels 0-6 (28 digit pairs): the pairs dropped at level 7 add at most ~2^-49 of
-// the column-scale product per row, with random signs over the rows of a Gram.
-#define GR_LEVELS 7
+// Levels 0-7 (34 digit pairs, 8 x 64 TMEM columns), as the linear combination:
+// the dropped pairs (level >= 8) add at most 2^-57.4 of the column-scale product
+// 2^(e+f) per row, so over n rows the error stays below 2^-57.4 n 2^(e+f) even
+// when every row drops the same amount (e.g. constant columns) -- far below the
+// FP64 summation error of the same Gram. Levels 3-7 are summed in units of level 7
+// (2^-56) and carried into the level 0-2 sum (units 2^-16) after every chunk, so
+// neither int64 sum can overflow for the 2^20 rows a split may hold.
+#define GR_LEVELS 8
 #define GR_SMEM (2 * TC_STAGE + TC_HDR)
 
 // grid (ceil(k1 / 128), ceil(k2 / 64), splits); part[split][i + j k1] = the
@@ -288,7 +300,7 @@ __global__ void k_fill_int(int *p, int count, int v)
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const double *__restrict__ W, long ldw,
           const int *__restrict__ ev, const int *__restrict__ ew, double *__restrict__ part, long rows_per_split,
-          int sym, int *__restrict__ err)
+          int sym, int *__restrict__ err, int stall)
 {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     uint8_t *sm = tc_smem;
@@ -346,7 +358,7 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
         const int buf = s & 1, cs = s % TC_CHUNK_STAGES;
         const bool chunk_end = cs == TC_CHUNK_STAGES - 1 || s == nst - 1;
         if (mma_warp) {
-            if (lane == 0) tc_issue_stage<GR_LEVELS, false>(h, sbase, tmem, N, s, cs, commits, err);
+            if (lane == 0) tc_issue_stage<GR_LEVELS, false>(h, sbase, tmem, N, s, cs, commits, err, stall);
             __syncwarp();
         } else {
             if (s >= 2 && !tc_mbar_wait(tc_smem_addr(h->bar) + 16 + 8 * buf, ((s >> 1) - 1) & 1, TC_WAIT_NS))
@@ -386,8 +398,10 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
                         for (int L = 0; L < GR_LEVELS; ++L) lev[L] = __uint_as_float(v[L][q]);
                         long long a, b;
                         oz_levels_to_int<GR_LEVELS>(lev, a, b);
-                        hi[g4 * 4 + q] += a;
-                        lo[g4 * 4 + q] += b;
+                        // lo < 2^40 before the chunk and a chunk's level 3-7 sum is < 2^56.1
+                        const long long l = lo[g4 * 4 + q] + b;
+                        hi[g4 * 4 + q] += a + (l >> 40);
+                        lo[g4 * 4 + q] = l & ((1LL << 40) - 1);
                     }
                 }
             }
@@ -406,7 +420,7 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
 #pragma unroll
             for (int q = 0; q < TC_COLS_PER_WARP; ++q) {
                 const int j = j0 + col0 + q;
-                if (j < k2) P[i + (long)j * k1] = oz_to_double<32>(hi[q], lo[q], e + ew[j] - OZ_SCALE_OFFSET);
+                if (j < k2) P[i + (long)j * k1] = oz_to_double<40>(hi[q], lo[q], e + ew[j] - OZ_SCALE_OFFSET);
             }
         }
     }
@@ -432,8 +446,9 @@ extern "C" int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double
         for (int b = 0; b < tj; ++b)
             if (!sym || a * TC_M <= b * TC_N + TC_N - 1) ++tiles;
     if (tiles < 1) tiles = 1;
-    // about one CTA per SM; int64 headroom: a row adds < 2^40 to the level 3-6
-    // sum (units of 2^-48), so a split holds at most 2^20 rows
+    // about one CTA per SM; int64 headroom: a row adds < 2^28.2 to the level 0-2
+    // sum (units of 2^-16), so a split holds at most 2^20 rows (the level 3-7 sum
+    // is carried into it after every chunk)
     long nsplit = ((long)ctx->num_sms + tiles - 1) / tiles;
     const long max_split = (n + 4 * TC_KS - 1) / (4 * TC_KS);
     if (nsplit > max_split) nsplit = max_split;
@@ -451,8 +466,10 @@ extern "C" int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double
     GB_LAUNCH(ctx, k_col_exponent, eg, 256, 0, n, k2, W, ldw, exps + k1);
     dim3 grid(ti, tj, (unsigned)nsplit);
     GB_PROF(ctx, GB_K_GRAM, 8.0 * n * (k1 + k2), sym ? 1.0 * n * k1 * (k1 + 1) : 2.0 * n * k1 * k2);
+    const int stall = ctx->tc_stall;
+    ctx->tc_stall = 0;
     GB_LAUNCH(ctx, k_gram_tc, grid, TC_THREADS, GR_SMEM, n, k1, k2, V, ldv, W, ldw, exps, exps + k1, ctx->scratch,
-              rps, sym, ctx->dev_err);
+              rps, sym, ctx->dev_err, stall);
     return gb_gram_reduce_launch(ctx, k1, k2, (int)nsplit, ctx->scratch, a_dev, lda, sym);
 }
 
@@ -547,7 +564,7 @@ template <bool MULTI>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, const uint4 *__restrict__ Bd,
              const int *__restrict__ g_in, const int *__restrict__ ec, double alpha, double beta,
-             double *__restrict__ Y, long ldy, int nst, int *__restrict__ err)
+             double *__restrict__ Y, long ldy, int nst, int *__restrict__ err, int stall)
 {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     uint8_t *sm = tc_smem;
@@ -665,7 +682,7 @@ k_lincomb_tc(int n, int k1, int k2, const double *__restrict__ X, long ldx, cons
             const int buf = gsc & 1, cs = s % chunk_stages;
             const bool chunk_end = cs == chunk_stages - 1 || s == nst - 1;
             if (mma_warp) {
-                if (lane == 0) tc_issue_stage<LC_LEVELS, true>(h, sbase, tmem, N, gsc, cs, commits, err);
+                if (lane == 0) tc_issue_stage<LC_LEVELS, true>(h, sbase, tmem, N, gsc, cs, commits, err, stall);
                 __syncwarp();
             } else {
                 if (gsc >= 2 && !tc_mbar_wait(tc_smem_addr(h->bar) + 16 + 8 * buf, ((gsc >> 1) - 1) & 1,
@@ -822,11 +839,13 @@ extern "C" int gb_lincomb_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const dou
     long P = ctx->num_sms / jtiles;
     if (P < 1) P = 1;
     if (P > ntiles) P = ntiles;
+    const int stall = ctx->tc_stall;
+    ctx->tc_stall = 0;
     if (k1 > OZ_EXACT_TERMS)
         GB_LAUNCH(ctx, k_lincomb_tc<true>, dim3((unsigned)P, jtiles), TC_THREADS, LC_SMEM, n, k1, k2, X, ldx,
-                  (const uint4 *)Bd, g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err);
+                  (const uint4 *)Bd, g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err, stall);
     else
         GB_LAUNCH(ctx, k_lincomb_tc<false>, dim3((unsigned)P, jtiles), TC_THREADS, LC_SMEM, n, k1, k2, X, ldx,
-                  (const uint4 *)Bd, g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err);
+                  (const uint4 *)Bd, g, ec, alpha, beta, Y, ldy, nst, ctx->dev_err, stall);
     return GCGE_GPU_OK;
 }

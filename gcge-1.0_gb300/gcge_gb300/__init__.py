@@ -103,6 +103,7 @@ def load():
         "GCGE_GPU_ProfileRead": (_I, [_P, _I, _P, _P, _P, _P, _I]),
         "GCGE_GPU_SetTensorEmulation": (_I, [_P, _I]),
         "GCGE_GPU_SetPairSpMM": (_I, [_P, _I]),
+        "GCGE_GPU_TestStallTensorWait": (_I, [_P, _I]),
         "GCGE_GPU_InnerProdNoAlloc": (_I, [_I, _I, _I, _P, C.c_long, _P, C.c_long, _P, _I, _I, _P]),
         "GCGE_GPU_PatternGrad": (_I, [_P, _P, _I, _P, _I, _I, _P, _I, _P]),
         "GCGE_GPU_EigvecAdjoint": (_I, [_P, _P, _P, _I, _P, _I, _P, _I, _P, _I, _D, _D, _I, C.POINTER(_I)]),

@@ -111,6 +111,17 @@ int  GCGE_GPU_MultiVecSetRandomValue(gcge_gpu_mv *mv, int start, int nvec, unsig
  * reference (its dense work is host BLAS). */
 int  GCGE_GPU_SetTensorEmulation(gcge_gpu_ctx *ctx, int on);
 
+/* Test hook for the failure path of the tensor-core kernels (no counterpart in
+ * the reference). With on != 0, the next tensor-core launch on this context
+ * (Gram or linear combination) has its MMA-issuing thread wait, before the first
+ * stage, for an arrival that cannot come, so that its bounded wait (1 s of
+ * %globaltimer) runs out: the CTAs take the timeout path (wait, bounded, for
+ * their own copies in flight, free their TMEM, return), the context's device
+ * error word is set, GCGE_GPU_Synchronize reports GCGE_GPU_ERR_TIMEOUT, and
+ * later tensor-core launches on this context do no work. One-shot: the flag is
+ * cleared by that launch. No fault, trap or endless wait is involved. */
+int  GCGE_GPU_TestStallTensorWait(gcge_gpu_ctx *ctx, int on);
+
 /* Sparse products Y = A X with two or more columns either in FP32-pair
  * arithmetic (on = 1: values as hi + lo floats, error-free products and sums on
  * the FP32 pipe, ~1e-14 of sum |a_ij x_j|; |x| >= 2^100 or non-finite X falls

@@ -1047,14 +1047,14 @@ static int solve_core(void *A, void *B, int n, const gcge_oracle_params *p, doub
     g->ev_max_it = p->ev_max_it; g->cg_max_it = p->cg_max_it; g->max_reorth_time = p->max_reorth_time;
     g->dirichlet = p->dirichlet_boundary; g->print_level = p->print_level;
     g->opt_rr_eig_partly = p->opt_rr_eig_partly;
-    strncpy(g->w_orth_type, p->w_orth_type[0] ? p->w_orth_type : "multi", 7);
+    snprintf(g->w_orth_type, sizeof g->w_orth_type, "%.7s", p->w_orth_type[0] ? p->w_orth_type : "multi");
     g->multi_tol_for_lock = 1e-6;                 /* src/gcge_para.c:59 */
     g->ev_tol = p->ev_tol; g->cg_rate = p->cg_rate;
     g->orth_zero_tol = p->orth_zero_tol + DBL_EPSILON;
     g->reorth_tol = p->reorth_tol;
     g->scbgs_reorth_tol = p->scbgs_reorth_tol + DBL_EPSILON;
     g->criterion_tol = p->criterion_tol;
-    strncpy(g->conv_type, p->conv_type, 3);
+    snprintf(g->conv_type, sizeof g->conv_type, "%.3s", p->conv_type);
     g->num_unlock = nev;
     g->res = (double *)malloc(sizeof(double) * nev);
     for (int i = 0; i < nev; ++i) g->res[i] = 1.0;
@@ -1349,4 +1349,115 @@ void gcge_oracle_table_mv_destroy(void *table, void ***mv, int k)
 void gcge_oracle_host_mv_read(void **mv, int k, int n, double *out)
 {
     for (int j = 0; j < k; ++j) memcpy(out + (size_t)j * n, hcol(mv[j]), sizeof(double) * n);
+}
+
+/* ------------------------------------------------ double-double checkers */
+/* Error-free transformations (Knuth's TwoSum, the fused multiply-add form of
+ * TwoProduct; Dekker, Numer. Math. 18, 1971) and double-double sums, used by the
+ * finite-difference check of the gradients: eigenvalues of a perturbed problem
+ * as Rayleigh quotients and eigenvectors refined by one correction step, both
+ * far more accurate than one FP64 rounding of the loss. Not a reference
+ * restatement: checker arithmetic only. */
+typedef struct { double hi, lo; } dd_t;
+
+static void two_sum(double a, double b, double *s, double *e)
+{
+    double x = a + b, bv = x - a, av = x - bv;
+    *s = x;
+    *e = (a - av) + (b - bv);
+}
+static dd_t dd_norm(double s, double e)
+{
+    dd_t r;
+    r.hi = s + e;
+    r.lo = e - (r.hi - s);
+    return r;
+}
+static dd_t dd_add(dd_t a, dd_t b)
+{
+    double s, e;
+    two_sum(a.hi, b.hi, &s, &e);
+    return dd_norm(s, e + (a.lo + b.lo));
+}
+static dd_t dd_prod(double a, double b)
+{
+    dd_t r;
+    r.hi = a * b;
+    r.lo = fma(a, b, -r.hi);
+    return r;
+}
+static dd_t dd_mul(dd_t a, dd_t b)
+{
+    dd_t p = dd_prod(a.hi, b.hi);
+    return dd_norm(p.hi, p.lo + (a.hi * b.lo + a.lo * b.hi));
+}
+static dd_t dd_div(dd_t a, dd_t b)
+{
+    double q1 = a.hi / b.hi;
+    dd_t r = dd_add(a, dd_mul(b, (dd_t){-q1, 0.0}));
+    double q2 = r.hi / b.hi;
+    r = dd_add(r, dd_mul(b, (dd_t){-q2, 0.0}));
+    double q3 = r.hi / b.hi;
+    dd_t q = dd_norm(q1, q2);
+    return dd_add(q, (dd_t){q3, 0.0});
+}
+/* (A x)_i with x = xh + xl, in double-double */
+static dd_t dd_row(const int *rp, const int *ci, const double *v, int i, const double *xh, const double *xl)
+{
+    dd_t y = {0.0, 0.0};
+    for (int j = rp[i]; j < rp[i + 1]; ++j) {
+        y = dd_add(y, dd_prod(v[j], xh[ci[j]]));
+        if (xl) y = dd_add(y, dd_prod(v[j], xl[ci[j]]));
+    }
+    return y;
+}
+
+/* out[0..1] = (x^T A x) / (x^T x) in double-double, x = xh + xl (xl may be NULL) */
+void gcge_oracle_dd_rayleigh(int n, const int *rp, const int *ci, const double *v, const double *xh,
+                             const double *xl, double *out)
+{
+    dd_t xax = {0.0, 0.0}, xx = {0.0, 0.0};
+    for (int i = 0; i < n; ++i) {
+        dd_t xi = {xh[i], xl ? xl[i] : 0.0};
+        xax = dd_add(xax, dd_mul(dd_row(rp, ci, v, i, xh, xl), xi));
+        xx = dd_add(xx, dd_mul(xi, xi));
+    }
+    dd_t q = dd_div(xax, xx);
+    out[0] = q.hi;
+    out[1] = q.lo;
+}
+
+/* r = A x - theta x, formed in double-double and rounded once per entry */
+void gcge_oracle_dd_residual(int n, const int *rp, const int *ci, const double *v, const double *xh,
+                             const double *xl, double th_hi, double th_lo, double *r)
+{
+    dd_t th = {-th_hi, -th_lo};
+    for (int i = 0; i < n; ++i) {
+        dd_t xi = {xh[i], xl ? xl[i] : 0.0};
+        dd_t y = dd_add(dd_row(rp, ci, v, i, xh, xl), dd_mul(th, xi));
+        r[i] = y.hi + y.lo;
+    }
+}
+
+/* x += d in double-double (x = xh + xl) */
+void gcge_oracle_dd_add_vec(int n, double *xh, double *xl, const double *d)
+{
+    for (int i = 0; i < n; ++i) {
+        dd_t x = dd_add((dd_t){xh[i], xl[i]}, (dd_t){d[i], 0.0});
+        xh[i] = x.hi;
+        xl[i] = x.lo;
+    }
+}
+
+/* out[0..3] = sum_i w_i x_i^2 and sum_i x_i^2 in double-double, x = xh + xl */
+void gcge_oracle_dd_weighted_sq(int n, const double *w, const double *xh, const double *xl, double *out)
+{
+    dd_t s = {0.0, 0.0}, t = {0.0, 0.0};
+    for (int i = 0; i < n; ++i) {
+        dd_t xi = {xh[i], xl ? xl[i] : 0.0};
+        dd_t x2 = dd_mul(xi, xi);
+        s = dd_add(s, dd_mul(x2, (dd_t){w[i], 0.0}));
+        t = dd_add(t, x2);
+    }
+    out[0] = s.hi; out[1] = s.lo; out[2] = t.hi; out[3] = t.lo;
 }

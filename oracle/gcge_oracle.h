@@ -99,6 +99,17 @@ int  gcge_oracle_table_mv_create(void *table, void *mat, int k, void ***mv);
 void gcge_oracle_table_mv_destroy(void *table, void ***mv, int k);
 void gcge_oracle_host_mv_read(void **mv, int k, int n, double *out);
 
+/* ---- double-double checker arithmetic (finite-difference checks) ----
+ * Rayleigh quotient (x^T A x)/(x^T x), residual A x - theta x, x += d and
+ * (sum w_i x_i^2, sum x_i^2), with x = xh + xl held as a double-double vector
+ * (xl may be NULL) and every sum formed by error-free transformations. */
+void gcge_oracle_dd_rayleigh(int n, const int *rp, const int *ci, const double *v, const double *xh,
+                             const double *xl, double *out);
+void gcge_oracle_dd_residual(int n, const int *rp, const int *ci, const double *v, const double *xh,
+                             const double *xl, double th_hi, double th_lo, double *r);
+void gcge_oracle_dd_add_vec(int n, double *xh, double *xl, const double *d);
+void gcge_oracle_dd_weighted_sq(int n, const double *w, const double *xh, const double *xl, double *out);
+
 /* ---- single operations, for per-kernel parity ---- */
 
 /* y = A x  (app/csr/gcge_app_csr.c:297-323) */

@@ -113,6 +113,45 @@ class Oracle(_Lib):
         L.gcge_oracle_table_mv_create.restype = C.c_int
         L.gcge_oracle_table_mv_destroy.argtypes = [VP, C.POINTER(VP), C.c_int]
         L.gcge_oracle_host_mv_read.argtypes = [VP, C.c_int, C.c_int, VP]
+        L.gcge_oracle_dd_rayleigh.argtypes = [C.c_int, _I, _I, _D, _D, VP, _D]
+        L.gcge_oracle_dd_residual.argtypes = [C.c_int, _I, _I, _D, _D, VP, C.c_double, C.c_double, _D]
+        L.gcge_oracle_dd_add_vec.argtypes = [C.c_int, _D, _D, _D]
+        L.gcge_oracle_dd_weighted_sq.argtypes = [C.c_int, _D, _D, VP, _D]
+
+    # ---- double-double checker arithmetic (x = xh + xl; xl may be None)
+    @staticmethod
+    def _csr(A):
+        return (np.ascontiguousarray(A.rowptr, dtype=np.int32), np.ascontiguousarray(A.col, dtype=np.int32),
+                np.ascontiguousarray(A.val, dtype=np.float64))
+
+    def dd_rayleigh(self, A, xh, xl=None):
+        """(x^T A x) / (x^T x) as a double-double pair (hi, lo)."""
+        rp, ci, v = self._csr(A)
+        out = np.zeros(2)
+        self.lib.gcge_oracle_dd_rayleigh(A.n, rp, ci, v, np.ascontiguousarray(xh, dtype=np.float64),
+                                         _ptr(None if xl is None else np.ascontiguousarray(xl)), out)
+        return float(out[0]), float(out[1])
+
+    def dd_residual(self, A, xh, xl, theta):
+        """A x - theta x (theta a double-double pair), rounded once per entry."""
+        rp, ci, v = self._csr(A)
+        r = np.zeros(A.n)
+        self.lib.gcge_oracle_dd_residual(A.n, rp, ci, v, np.ascontiguousarray(xh, dtype=np.float64),
+                                         _ptr(None if xl is None else np.ascontiguousarray(xl)), theta[0],
+                                         theta[1], r)
+        return r
+
+    def dd_add_vec(self, xh, xl, d):
+        """x += d in place (x = xh + xl, both contiguous float64 arrays)."""
+        self.lib.gcge_oracle_dd_add_vec(len(xh), xh, xl, np.ascontiguousarray(d, dtype=np.float64))
+
+    def dd_weighted_sq(self, w, xh, xl=None):
+        """((sum w x^2) hi, lo, (sum x^2) hi, lo)."""
+        out = np.zeros(4)
+        self.lib.gcge_oracle_dd_weighted_sq(len(xh), np.ascontiguousarray(w, dtype=np.float64),
+                                            np.ascontiguousarray(xh, dtype=np.float64),
+                                            _ptr(None if xl is None else np.ascontiguousarray(xl)), out)
+        return tuple(float(t) for t in out)
 
     # ---- GCGE's solver core over a GCGE_OPS table (the drop-in boundary)
     def new_table(self, host=False):

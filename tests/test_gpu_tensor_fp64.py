@@ -182,3 +182,42 @@ def test_tensor_lincomb_compensating_scales(ctx):
         for j in (0, 17, k2 - 1):
             ex = exact_dot(X[r], C[:, j])
             assert abs(y_tc[r, j] - ex) <= 2.0 ** -52 * abs(ex) + bound[r, j]
+
+
+@pytest.mark.parametrize("pattern", ["same_sign", "cancelling"])
+def test_tensor_gram_at_full_size_against_exact(ctx, pattern):
+    """Adversarial Gram at the 160^3 size (n = 4,096,000) with an exact answer.
+    Constant columns make every row drop the same digit pairs, so the dropped mass
+    adds up coherently over all n rows (the worst case of the splitting): V[:, i] =
+    c_i, W[:, j] = d_j on every row (same sign) or d_j on even rows and -d'_j =
+    -fl(d_j (1 + 2^-20)) on odd rows (a 2^20-fold cancellation). The entries carry
+    full 53-bit significands, so every digit level is populated. Bound: one final
+    rounding plus n 2^-57.4 2^(e+f) for the dropped pairs (levels >= 8)."""
+    n, k1, k2 = 4096000, 128, 64
+    rng = np.random.default_rng(41)
+    c = rng.uniform(0.5, 1.0, k1) * 2.0 ** rng.integers(-3, 4, k1)
+    d = rng.uniform(0.5, 1.0, k2) * 2.0 ** rng.integers(-3, 4, k2)
+    V = np.broadcast_to(c, (n, k1))
+    if pattern == "same_sign":
+        W = np.broadcast_to(d, (n, k2))
+        exact = [[Fraction(n) * Fraction(ci) * Fraction(dj) for dj in d] for ci in c]
+    else:
+        dp = d * (1.0 + 2.0 ** -20)
+        W = np.empty((n, k2))
+        W[0::2] = d
+        W[1::2] = -dp
+        exact = [[Fraction(n // 2) * Fraction(ci) * (Fraction(dj) - Fraction(dpj)) for dj, dpj in zip(d, dp)]
+                 for ci in c]
+    got = gram(ctx, np.ascontiguousarray(V), W)
+    e = np.frexp(c)[1]                                   # column scales: |x| < 2^e
+    f = np.frexp(np.max(np.abs(W[:2]), axis=0))[1]
+    worst = 0.0
+    for i in range(k1):
+        for j in range(k2):
+            ex = exact[i][j]
+            err = float(abs(Fraction(got[i, j]) - ex))
+            bound = float(abs(ex)) * 2.0 ** -52 + n * 2.0 ** (-57.4 + e[i] + f[j])
+            assert err <= bound, (pattern, i, j, err, bound)
+            worst = max(worst, err / float(abs(ex)))
+    # far inside the FP64 summation error of the same Gram (same sign: ~n eps / nsplit relative)
+    assert worst < (1e-15 if pattern == "same_sign" else 1e-10), worst
