@@ -120,6 +120,22 @@ extern "C" int gb_set_diag_from(gcge_gpu_ctx *ctx, double *H, int ldh, int count
     GB_LAUNCH(ctx, k_set_diag, (count + 255) / 256, 256, 0, H, ldh, count, vals);
     return GCGE_GPU_OK;
 }
+// A-orthogonal mode: the projected eigenvalues nu of -V^T B V (ascending) are
+// kept in nu and turned into lambda = -1/nu (ascending as well)
+__global__ void k_neg_recip(int count, double *v, double *nu)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const double x = v[i];
+        nu[i] = x;
+        v[i] = -1.0 / x;
+    }
+}
+extern "C" int gb_neg_recip(gcge_gpu_ctx *ctx, int count, double *v, double *nu)
+{
+    if (count <= 0) return GCGE_GPU_OK;
+    GB_LAUNCH(ctx, k_neg_recip, (count + 255) / 256, 256, 0, count, v, nu);
+    return GCGE_GPU_OK;
+}
 // soft locking: H[0:s, w0:m] = H[w0:m, 0:s] = 0 (the W block decoupled from the s
 // locked Ritz vectors); C[:, 0:s] = e_0 .. e_(s-1); C[0:s, s:iu] = 0
 __global__ void k_soft_lock(double *H, int ldh, int m, int w0, int s, double *C, int ldc, int iu)

@@ -209,6 +209,8 @@ int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int il, int iu,
 int gb_set_zero(gcge_gpu_ctx *ctx, double *a, size_t count);
 int gb_copy_d(gcge_gpu_ctx *ctx, double *dst, const double *src, size_t count);
 int gb_set_diag_from(gcge_gpu_ctx *ctx, double *H, int ldh, int count, const double *vals);
+/* nu[i] = v[i], v[i] = -1 / v[i] for i < count (A-orthogonal Rayleigh-Ritz) */
+int gb_neg_recip(gcge_gpu_ctx *ctx, int count, double *v, double *nu);
 int gb_symmetrize_from_upper(gcge_gpu_ctx *ctx, double *H, int ldh, int m);
 /* soft locking of the first s Ritz vectors: H's W columns (from w0) decoupled from
  * them, C[:, 0:s] = identity columns, C[0:s, s:iu] = 0 */

@@ -295,11 +295,12 @@ __global__ void k_fill_int(int *p, int count, int v)
 #define GR_SMEM (2 * TC_STAGE + TC_HDR)
 
 // grid (ceil(k1 / 128), ceil(k2 / 64), splits); part[split][i + j k1] = the
-// split's FP64 partial of sum_r V[r, i] W[r, j] (sym: tiles wholly below the
-// diagonal are skipped).
+// split's exact integer sum of the digit products of sum_r V[r, i] W[r, j] as
+// (hi, lo), value (hi 2^40 + lo) 2^(e_i + f_j - 66) (sym: tiles wholly below
+// the diagonal are skipped).
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const double *__restrict__ W, long ldw,
-          const int *__restrict__ ev, const int *__restrict__ ew, double *__restrict__ part, long rows_per_split,
+          const int *__restrict__ ev, const int *__restrict__ ew, long long *__restrict__ part, long rows_per_split,
           int sym, int *__restrict__ err, int stall)
 {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
@@ -413,18 +414,47 @@ k_gram_tc(int n, int k1, int k2, const double *__restrict__ V, long ldv, const d
     }
 
     if (!*(volatile int *)&h->flag) {
+        // the split's exact integer sums (level 0-2 part, level 3-7 part < 2^40),
+        // summed exactly over the splits and rounded once by k_gram_reduce_oz
         const int i = i0 + quarter * 32 + lane;
-        double *P = part + (long)blockIdx.z * k1 * k2;
+        long long *P = part + 2 * (long)blockIdx.z * k1 * k2;
         if (i < k1) {
-            const int e = ev[i];
 #pragma unroll
             for (int q = 0; q < TC_COLS_PER_WARP; ++q) {
                 const int j = j0 + col0 + q;
-                if (j < k2) P[i + (long)j * k1] = oz_to_double<40>(hi[q], lo[q], e + ew[j] - OZ_SCALE_OFFSET);
+                if (j < k2) {
+                    P[2 * (i + (long)j * k1)] = hi[q];
+                    P[2 * (i + (long)j * k1) + 1] = lo[q];
+                }
             }
         }
     }
     tc_release(h, tmem, mma_warp, commits, nullptr);
+}
+
+// a[i + j lda] = the exact sum over the splits of their (hi 2^40 + lo) integer
+// sums, rounded once to FP64: every Gram entry is the correctly rounded value of
+// the exact sum of the split operands' kept digit products, whatever the row
+// split (sym: upper triangle computed, mirrored)
+__global__ void k_gram_reduce_oz(int k1, int k2, int nsplit, const long long *__restrict__ part,
+                                 const int *__restrict__ ev, const int *__restrict__ ew, double *__restrict__ a,
+                                 int lda, int sym)
+{
+    const long total = (long)k1 * k2;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % k1), j = (int)(t / k1);
+        if (sym && i > j) continue;
+        __int128 hs = 0;
+        long long ls = 0;                                // nsplit < 2^23 terms below 2^40 each
+        for (int q = 0; q < nsplit; ++q) {
+            hs += part[2 * ((long)q * total + t)];
+            ls += part[2 * ((long)q * total + t) + 1];
+        }
+        const __int128 z = hs * ((__int128)1 << 40) + ls;
+        const double s = z == 0 ? 0.0 : oz_i128_to_double(z, ev[i] + ew[j] - OZ_SCALE_OFFSET - 56);
+        a[i + (long)j * lda] = s;
+        if (sym && i != j) a[j + (long)i * lda] = s;
+    }
 }
 
 // a[i + j*lda] = sum_r V[r,i] W[r,j] to FP64 accuracy on the tensor cores.
@@ -458,7 +488,7 @@ extern "C" int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double
     long rps = ((n + nsplit - 1) / nsplit + TC_KS - 1) / TC_KS * TC_KS;
     nsplit = (n + rps - 1) / rps;
     if (nsplit < 1) nsplit = 1;
-    int st = gb_scratch(ctx, (size_t)nsplit * k1 * k2);
+    int st = gb_scratch(ctx, (size_t)2 * nsplit * k1 * k2);
     if (st) return st;
     GB_LAUNCH(ctx, k_fill_int, (k1 + k2 + 127) / 128, 128, 0, exps, k1 + k2, OZ_NO_EXP);
     const int eg = ctx->num_sms * 4;
@@ -468,9 +498,13 @@ extern "C" int gb_gram_tc(gcge_gpu_ctx *ctx, int n, int k1, int k2, const double
     GB_PROF(ctx, GB_K_GRAM, 8.0 * n * (k1 + k2), sym ? 1.0 * n * k1 * (k1 + 1) : 2.0 * n * k1 * k2);
     const int stall = ctx->tc_stall;
     ctx->tc_stall = 0;
-    GB_LAUNCH(ctx, k_gram_tc, grid, TC_THREADS, GR_SMEM, n, k1, k2, V, ldv, W, ldw, exps, exps + k1, ctx->scratch,
-              rps, sym, ctx->dev_err, stall);
-    return gb_gram_reduce_launch(ctx, k1, k2, (int)nsplit, ctx->scratch, a_dev, lda, sym);
+    long long *part = reinterpret_cast<long long *>(ctx->scratch);
+    GB_LAUNCH(ctx, k_gram_tc, grid, TC_THREADS, GR_SMEM, n, k1, k2, V, ldv, W, ldw, exps, exps + k1, part, rps, sym,
+              ctx->dev_err, stall);
+    long rg = ((long)k1 * k2 + 255) / 256;
+    if (rg > (long)ctx->num_sms * 16) rg = (long)ctx->num_sms * 16;
+    GB_LAUNCH(ctx, k_gram_reduce_oz, (int)rg, 256, 0, k1, k2, (int)nsplit, part, exps, exps + k1, a_dev, lda, sym);
+    return GCGE_GPU_OK;
 }
 
 // ---------------------------------------------------------------- linear combination (tcgen05)

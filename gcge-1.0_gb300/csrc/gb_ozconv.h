@@ -70,6 +70,42 @@ OZ_HD double oz_to_double(long long hi, long long lo, int s)
     return oz_bits_to_double(sign | ((unsigned long long)(E + 1023) << 52) | (m & ((1ull << 52) - 1)));
 }
 
+// z 2^e0 rounded once to nearest-even, z any 128-bit integer (the exact sum of a
+// Gram entry's split partials, hi 2^40 + lo summed over the splits)
+OZ_HD double oz_i128_to_double(__int128 z, int e0)
+{
+    if (z == 0) return 0.0;
+    unsigned long long sign = 0;
+    if (z < 0) {
+        sign = 1ull << 63;
+        z = -z;
+    }
+    const unsigned __int128 u = (unsigned __int128)z;
+    const unsigned long long zh = (unsigned long long)(u >> 64), zl = (unsigned long long)u;
+    const int nb = zh ? 128 - oz_clz64(zh) : 64 - oz_clz64(zl);
+    int E = nb - 1 + e0;
+    unsigned long long m;
+    if (nb <= 53) {
+        m = zl << (53 - nb);
+    } else {
+        const int sh = nb - 53;
+        const unsigned __int128 q = u >> sh;
+        const unsigned __int128 rem = u - (q << sh);
+        const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        m = (unsigned long long)q;
+        if (rem > half || (rem == half && (m & 1))) ++m;
+        if (m >> 53) {
+            m >>= 1;
+            ++E;
+        }
+    }
+    if (E < -1022 || E > 1023) {                   // outside the normal range: scale in FP64
+        const double mag = ldexp((double)zh, e0 + 64) + ldexp((double)zl, e0);
+        return sign ? -mag : mag;
+    }
+    return oz_bits_to_double(sign | ((unsigned long long)(E + 1023) << 52) | (m & ((1ull << 52) - 1)));
+}
+
 // The same value for SH = 40 in 64-bit arithmetic, for |hi| < 2^41 and |lo| < 2^62
 // (eight levels of at most 2^24 each). z = hi 2^40 + lo = T 2^18 + R with T =
 // floor(z / 2^18) (|T| < 2^63) and 0 <= R < 2^18; |z| is carried as U 2^e where

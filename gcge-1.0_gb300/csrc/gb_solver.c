@@ -60,7 +60,7 @@ typedef struct {
     void *bcg_work;
     size_t bcg_bytes;
     /* device small dense */
-    double *H, *C, *Ctmp, *AApp, *Gs, *Ts, *chol_work, *eval_d, *eig_work, *res_d, *lam_d, *dsmall;
+    double *H, *C, *Ctmp, *AApp, *Gs, *Ts, *chol_work, *eval_d, *eig_work, *res_d, *lam_d, *dsmall, *nu_d;
     int *unlock_d, *kept_d, *info_d, *pos_d;
     /* host */
     double *eval_h, *res_h, *resv;
@@ -72,6 +72,8 @@ typedef struct {
     int dim_x, dim_xp, dim_xpw, last_dim_xpw, last_dim_x, unconv_bs, num_unlock, num_iter;
     double max_res, min_res, sum_res, conv_omega_norm, zero_tol;
     int orth_kind;             /* w_orth_type variant (gb_orth.h) */
+    int amode;                 /* orth_type "A": basis A-orthonormal, projected matrix -V^T B V */
+    const gcge_gpu_mat *Om;    /* the orthonormalisation matrix: B, or A in A-orthogonal mode */
     int soft_locked;           /* Ritz pairs soft-locked in the last Rayleigh-Ritz step */
     gb_orth_ws ows;
     phase_timer tm;
@@ -133,6 +135,7 @@ void GCGE_GPU_ParamsDefault(gcge_gpu_params *p)
     strcpy(p->w_orth_type, "multi");
     p->opt_rr_eig_partly = 0;
     p->multi_tol_for_lock = 1e-6;
+    strcpy(p->orth_type, "B");
     p->precision = 0;
     p->seed = 1;
 }
@@ -140,7 +143,10 @@ void GCGE_GPU_ParamsDefault(gcge_gpu_params *p)
 /* ------------------------------------------------------------ Rayleigh-Ritz */
 /* GCGE_ComputeSubspaceMatrix (src/gcge_rayleighritz.c:113-200): XAX = diag(eval),
  * XAP = 0, PAP = pp^T H_old pp, then [X,P,W]^T A W from one SpMM and two Grams;
- * H is kept fully symmetric (upper triangle mirrored). */
+ * H is kept fully symmetric (upper triangle mirrored). In A-orthogonal mode the
+ * basis is A-orthonormal and H = -V^T B V, whose smallest eigenvalues nu are
+ * the largest of V^T B V (lambda = -1/nu): its X block is diag(nu) of the last
+ * step and its W columns come from -B W. */
 static int rr_matrix(gcg_t *g)
 {
     gcge_gpu_ctx *ctx = g->ctx;
@@ -155,11 +161,16 @@ static int rr_matrix(gcg_t *g)
         if (dim_p > 0)
             TRY(gb_small_gemm(ctx, 'T', 'N', dim_p, dim_p, lde, 1.0, pp, lde, g->AApp, lde, 0.0,
                               g->H + (size_t)dim_x * ldm + dim_x, ldm));
-        TRY(gb_set_diag_from(ctx, g->H, ldm, dim_x, g->eval_d));
+        TRY(gb_set_diag_from(ctx, g->H, ldm, dim_x, g->amode ? g->nu_d : g->eval_d));
     }
-    /* VTAW (src/gcge_rayleighritz.c:35-81): AW = A W into S1 */
+    /* VTAW (src/gcge_rayleighritz.c:35-81): AW = A W into S1 (A-orthogonal mode: -B W) */
     const int w_len = ldm - dim_xp, xp_len = dim_xp;
-    TRY(gb_spmm(ctx, g->A, g->V + dim_xp, g->ldv, g->S1, g->lds, w_len, 1.0, NULL, 0.0, NULL));
+    if (!g->amode)
+        TRY(gb_spmm(ctx, g->A, g->V + dim_xp, g->ldv, g->S1, g->lds, w_len, 1.0, NULL, 0.0, NULL));
+    else if (g->B)
+        TRY(gb_spmm(ctx, g->B, g->V + dim_xp, g->ldv, g->S1, g->lds, w_len, -1.0, NULL, 0.0, NULL));
+    else
+        TRY(gb_axpby(ctx, n, w_len, -1.0, g->V + dim_xp, g->ldv, 0.0, g->S1, g->lds));
     /* [X P W]^T (A W) in one Gram: H[0:ldm, dim_xp:ldm] (the W^T A W block in full;
      * its lower half is then replaced by the mirrored upper half) */
     (void)xp_len;
@@ -171,8 +182,21 @@ fail:
 }
 
 /* GCGE_ComputeSubspaceEigenpairs (src/gcge_rayleighritz.c:364-590) with
- * opt_rr_eig_partly = 0: eigenpairs 1 .. min(max_dim_x, ldm). */
+ * opt_rr_eig_partly = 0: eigenpairs 1 .. min(max_dim_x, ldm). In A-orthogonal
+ * mode the eigenvalues nu of -V^T B V come out ascending; lambda = -1/nu keeps
+ * that order (the reference solves V^T B V for its smallest eigenvalues and
+ * reverses them with GCGE_SortEigenpairs, src/gcge_rayleighritz.c:581-617,
+ * which picks the wrong end of its spectrum). */
+static int rr_eig_solve(gcg_t *g);
 static int rr_eig(gcg_t *g)
+{
+    const int ldm = g->dim_xpw, iu = g->max_dim_x < ldm ? g->max_dim_x : ldm;
+    int st = rr_eig_solve(g);
+    if (st || !g->amode) return st;
+    const int s = g->soft_locked;
+    return gb_neg_recip(g->ctx, iu - s, g->eval_d + s, g->nu_d + s);
+}
+static int rr_eig_solve(gcg_t *g)
 {
     const int ldm = g->dim_xpw;
     const int iu = g->max_dim_x < ldm ? g->max_dim_x : ldm;
@@ -426,7 +450,7 @@ static void gcg_free(gcg_t *g)
 {
     void *dev[] = {g->V, g->S1, g->S2, g->S3, g->bcg_work, g->H, g->C, g->Ctmp, g->AApp, g->Gs, g->Ts,
                    g->chol_work, g->eval_d, g->eig_work, g->res_d, g->lam_d, g->dsmall, g->unlock_d, g->kept_d,
-                   g->info_d, g->pos_d};
+                   g->info_d, g->pos_d, g->nu_d};
     for (size_t i = 0; i < sizeof(dev) / sizeof(dev[0]); ++i)
         if (dev[i]) gb_dev_free(g->ctx, dev[i]);
     gb_orth_ws_free(&g->ows);
@@ -449,7 +473,9 @@ int GCGE_GPU_Solve(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_mat 
 {
     if (!ctx || !A || !pin || !eval || !evec) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     if (pin->nev <= 0 || pin->nev > A->n || evec->ncols < pin->nev || evec->n != A->n || (B && B->n != A->n) ||
-        (pin->precision && !A->v32) || pin->precision < 0 || pin->precision > 2 || pin->block_size < 0)
+        (pin->precision && !A->v32) || pin->precision < 0 || pin->precision > 2 || pin->block_size < 0 ||
+        !(pin->orth_type[0] == '\0' || ((pin->orth_type[0] == 'A' || pin->orth_type[0] == 'B') &&
+                                       pin->orth_type[1] == '\0')))
         return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     /* precision 2: the outer products of the iteration (A W, B W, A X, B X) in
      * FP32-pair arithmetic for the duration of this solve */
@@ -476,6 +502,9 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
     g->zero_tol = pin->orth_zero_tol + DBL_EPSILON;
     g->p.w_orth_type[sizeof(g->p.w_orth_type) - 1] = '\0';
     g->orth_kind = gb_orth_kind(g->p.w_orth_type);
+    g->p.orth_type[sizeof(g->p.orth_type) - 1] = '\0';
+    g->amode = g->p.orth_type[0] == 'A';
+    g->Om = g->amode ? A : B;
     const int nev = g->nev, n = g->n;
     /* GCGE_WORKSPACE_Setup sizes (src/gcge_workspace.c:61-73) */
     {
@@ -509,7 +538,7 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
         dmalloc(ctx, (void **)&g->res_d, sizeof(double) * 3 * (nev + 8)) || dmalloc(ctx, (void **)&g->lam_d, sizeof(double) * (vs + 8)) ||
         dmalloc(ctx, (void **)&g->dsmall, sizeof(double) * 64) || dmalloc(ctx, (void **)&g->unlock_d, sizeof(int) * vs) ||
         dmalloc(ctx, (void **)&g->kept_d, sizeof(int) * 4) || dmalloc(ctx, (void **)&g->info_d, sizeof(int) * 4) ||
-        dmalloc(ctx, (void **)&g->pos_d, sizeof(int) * vs)) {
+        dmalloc(ctx, (void **)&g->pos_d, sizeof(int) * vs) || dmalloc(ctx, (void **)&g->nu_d, sizeof(double) * vs)) {
         st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
         goto fail;
     }
@@ -524,6 +553,7 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
     if (!g->eval_h || !g->res_h || !g->resv || !g->unlock_h || !g->pos_h) { st = gb_fail(ctx, GCGE_GPU_ERR_NOMEM); goto fail; }
     CTRY(cudaMemsetAsync(g->V, 0, sizeof(double) * (size_t)n * g->ldv, ctx->stream));
     CTRY(cudaMemsetAsync(g->eval_d, 0, sizeof(double) * vs, ctx->stream));
+    CTRY(cudaMemsetAsync(g->nu_d, 0, sizeof(double) * vs, ctx->stream));
     CTRY(cudaMemsetAsync(g->info_d, 0, sizeof(int), ctx->stream));
     TRY(gb_scratch(ctx, (size_t)4 * vs2 + (size_t)((n + 1023) / 1024) * 3 * (vs + 8) + (1 << 16)));
     /* GCGE_PARA_Setup (src/gcge_para.c:357-386) */
@@ -547,7 +577,8 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
         int have = 0;
         if (pin->given_init_evec) {
             int end = nev;
-            TRY(gb_orthonormalize(ctx, n, g->X, g->ldx, 0, &end, B, g->p.max_reorth_time, g->zero_tol, &g->ows));
+            TRY(gb_orthonormalize(ctx, n, g->X, g->ldx, 0, &end, g->Om, g->p.max_reorth_time, g->zero_tol,
+                                  &g->ows));
             have = end;
         }
         for (int attempt = 0; have < nev && attempt < 16; ++attempt) {
@@ -570,7 +601,8 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
             }
             if (pin->dirichlet_boundary) TRY(gb_dirichlet_zero(ctx, A, B, nev - have, g->X + have, g->ldx));
             int end = nev;
-            TRY(gb_orthonormalize(ctx, n, g->X, g->ldx, have, &end, B, g->p.max_reorth_time, g->zero_tol, &g->ows));
+            TRY(gb_orthonormalize(ctx, n, g->X, g->ldx, have, &end, g->Om, g->p.max_reorth_time, g->zero_tol,
+                                  &g->ows));
             have = end;
         }
         if (have < nev) { st = gb_fail(ctx, GCGE_GPU_ERR_BREAKDOWN); goto fail; }
@@ -601,8 +633,8 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
     g->last_dim_xpw = g->dim_xpw;
     g->dim_xpw = g->dim_xp + g->unconv_bs;
     ph_begin(g, PH_W_ORTH);
-    TRY(gb_orthonormalize_kind(ctx, n, g->V, g->ldv, g->dim_x, &g->dim_xpw, B, g->p.max_reorth_time, g->zero_tol,
-                               &g->ows, g->orth_kind));
+    TRY(gb_orthonormalize_kind(ctx, n, g->V, g->ldv, g->dim_x, &g->dim_xpw, g->Om, g->p.max_reorth_time,
+                               g->zero_tol, &g->ows, g->orth_kind));
     ph_end(g);
     g->dim_xp = nev;
     ph_begin(g, PH_RR_MAT);
@@ -630,7 +662,7 @@ static int solve_impl(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, const gcge_gpu_m
             g->last_dim_xpw = g->dim_xpw;
             g->dim_xpw = g->dim_xp + g->unconv_bs;
             ph_begin(g, PH_W_ORTH);
-            TRY(gb_orthonormalize_kind(ctx, n, g->V, g->ldv, g->dim_xp, &g->dim_xpw, B, g->p.max_reorth_time,
+            TRY(gb_orthonormalize_kind(ctx, n, g->V, g->ldv, g->dim_xp, &g->dim_xpw, g->Om, g->p.max_reorth_time,
                                        g->zero_tol, &g->ows, g->orth_kind));
             ph_end(g);
             ph_begin(g, PH_RR_MAT);

@@ -36,7 +36,7 @@ class Params(C.Structure):
                 ("ev_tol", C.c_double), ("cg_rate", C.c_double), ("orth_zero_tol", C.c_double),
                 ("conv_type", C.c_char * 4), ("precision", C.c_int), ("seed", C.c_ulonglong),
                 ("print_level", C.c_int), ("precond", C.c_int), ("w_orth_type", C.c_char * 8),
-                ("opt_rr_eig_partly", C.c_int), ("multi_tol_for_lock", C.c_double)]
+                ("opt_rr_eig_partly", C.c_int), ("multi_tol_for_lock", C.c_double), ("orth_type", C.c_char * 4)]
 
 
 class Stats(C.Structure):
@@ -239,7 +239,7 @@ class Context:
         p = Params()
         self.lib.GCGE_GPU_ParamsDefault(C.byref(p))
         for k, v in kw.items():
-            if k in ("conv_type", "w_orth_type"):
+            if k in ("conv_type", "w_orth_type", "orth_type"):
                 v = v.encode()
             setattr(p, k, v)
         return p

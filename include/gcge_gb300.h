@@ -212,6 +212,14 @@ typedef struct {
                                  only the trailing projected block is solved      */
     double multi_tol_for_lock;/* 1e-6: relative gap under which an earlier
                                  eigenvalue is taken as a multiple of it          */
+    char   orth_type[4];      /* "B" (default): the basis is B-orthonormal and the
+                                 Rayleigh-Ritz matrix is V^T A V; "A": the basis is
+                                 A-orthonormal (A must be positive definite), the
+                                 projected matrix is V^T B V, whose largest
+                                 eigenvalues mu give lambda = 1/mu (the role of
+                                 orth_type "A", src/gcge_eigsol.c:100-113, with
+                                 GCGE_SortEigenpairs, src/gcge_rayleighritz.c:581-617);
+                                 the eigenvectors are returned A-orthonormal      */
 } gcge_gpu_params;
 
 typedef struct {
