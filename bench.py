@@ -351,6 +351,8 @@ def run_gb300(args, dist):
             fp64_iters.append(st64.num_iter)
     fp64_s = dist.max(sum(fp64_times) / len(fp64_times)) if fp64_times else None
     res64, err64 = check_solution(A, B, ev64, X64, exact) if fp64_times else (None, None)
+    if not fp64_times:
+        X64 = None
     # ---- the precision-2 form (outer products in FP32-pair arithmetic): not the headline
     p2 = None
     if args.precision != 2 and fp64_times:
@@ -379,7 +381,7 @@ def run_gb300(args, dist):
     evj, Xj, stj = ctx.solve(dA, dB, pj, evec=X)
     resj, errj = check_solution(A, B, evj, Xj, exact)
     jacobi = {"s": sig(stj.solve_ms * 1e-3), "iters": stj.num_iter, "max_res": sig(resj, 3)}
-    del Xh, X64, Xj
+    Xh = X64 = Xj = None
     ctx.close()
     out = None
     if rank == 0:
