@@ -564,7 +564,8 @@ def run_kernel(args):
 
 
 def run_config(args, ctx):
-    """One mixed-precision solve of a large parity configuration, timed on the device,
+    """One mixed-precision solve of a large parity configuration, timed on the device
+    (kernel_ms: per class of the profiling mode, [ms, launches, achieved GB/s]),
     with every residual checked on the host: c3 = 7-point variable-coefficient
     diffusion on --nc^3 cells (sigma-1 Gaussian field, correlation length 8 cells,
     lumped diagonal mass U[1, 2]), nev 100, block 128; c5 = weighted power-law
@@ -587,14 +588,21 @@ def run_config(args, ctx):
     X = ctx.multivec(A.n, nev)
     params = ctx.params(nev=nev, block_size=block, ev_tol=1e-8, conv_type="BR", ev_max_it=args.max_it,
                         seed=20241203, precision=1, precond=args.precond)
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
     ev, Xh, st = ctx.solve(dA, dB, params, evec=X)
+    prof = ctx.profile_read(reset=True)
+    ctx.profile(False)
     As, Bs = A.to_scipy(), B.to_scipy()
     res = np.linalg.norm(As @ Xh - (Bs @ Xh) * ev[None, :], axis=0) / (np.abs(ev) * np.linalg.norm(Bs @ Xh, axis=0))
     out = {"kernel": args.kernel, "precond": args.precond,
            "shape": "%s: n=%d nnz(A)=%d, nev=%d, block=%d" % (desc, A.n, A.nnz, nev, block),
            "problem_generation_s": gen_s, "solve_s": st.solve_ms * 1e-3, "iterations": st.num_iter,
            "unconverged": st.num_unlock, "max_residual": float(res.max()), "lambda_min": float(ev[0]),
-           "lambda_max": float(ev[-1]), "phase_ms": st.as_dict()["phase_ms"]}
+           "lambda_max": float(ev[-1]), "phase_ms": st.as_dict()["phase_ms"],
+           "kernel_ms": {c: [round(v["ms"], 1), v["launches"],
+                             round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] > 0 else None]
+                         for c, v in prof.items() if v["launches"]}}
     if args.kernel == "c5":
         ctx.sync()
         t = time.perf_counter()
