@@ -223,7 +223,8 @@ extern "C" int gb_p_coef_assemble(gcge_gpu_ctx *ctx, double *coef, int ldc, int 
 // the kept rows/columns is inverted; T[K_q, p] = inv(U)[q, p] (zeros elsewhere).
 __global__ void __launch_bounds__(512)
 k_chol_deflate(int k, const double *__restrict__ G, int ldg, double *__restrict__ T, int *kept_out,
-               double zero_tol, double rel_tol, double *__restrict__ S, double *__restrict__ R)
+               double zero_tol, double rel_tol, double *__restrict__ S, double *__restrict__ R,
+               double *__restrict__ min_ratio)
 {
     extern __shared__ int shm[];
     int *keep = shm;            // k
@@ -237,11 +238,13 @@ k_chol_deflate(int k, const double *__restrict__ G, int ldg, double *__restrict_
         R[t] = 0.0;
     }
     __syncthreads();
+    double mr = 1.0;                                     // thread 0: smallest pivot / diagonal
     for (int j = 0; j < k; ++j) {
         if (tid == 0) {
             const double d = S[j + (long)j * k];
             const double g = G[j + (long)j * ldg];
             const bool ok = isfinite(d) && isfinite(g) && g > 0.0 && d > rel_tol * g && sqrt(d) > zero_tol;
+            if (g > 0.0) mr = fmin(mr, d / g);
             s_drop = ok ? 0 : 1;
             s_r = ok ? sqrt(d) : 0.0;
             keep[j] = ok;
@@ -263,6 +266,7 @@ k_chol_deflate(int k, const double *__restrict__ G, int ldg, double *__restrict_
         int c = 0;
         for (int j = 0; j < k; ++j) { pos[j] = keep[j] ? c : -1; c += keep[j]; }
         *kept_out = c;
+        if (min_ratio) *min_ratio = mr;
     }
     __syncthreads();
     // T = 0, then column p of inv(U) for each kept column j (p = pos[j]):
@@ -292,15 +296,17 @@ extern "C" int gb_chol_deflate(gcge_gpu_ctx *ctx, int k, const double *G, int ld
 {
     if (k <= 0) return GCGE_GPU_OK;
     double *S = work, *R = work + (size_t)k * k;
-    GB_LAUNCH(ctx, k_chol_deflate, 1, 512, 2 * k * sizeof(int), k, G, ldg, T, kept_dev, zero_tol, rel_tol, S, R);
+    GB_LAUNCH(ctx, k_chol_deflate, 1, 512, 2 * k * sizeof(int), k, G, ldg, T, kept_dev, zero_tol, rel_tol, S, R,
+              (double *)nullptr);
     return GCGE_GPU_OK;
 }
 
 // ---------------------------------------------------------------- eigensolver
-// work layout (doubles): Aw[m*m] | d[m] | e[m] | tau[m] | Zt[m*m] | lu[6*m*m] | scal[16]
+// work layout (doubles): Aw[m*m] | d[m] | e[m] | tau[m] | Zt[m*m] | Zq[m*m] | G[m*m] | Tq[m*m] |
+// cw[2*m*m] | 64 (the pivot ratio and kept count of the Cholesky-QR reorthogonalisation)
 extern "C" size_t gb_syevx_work_doubles(int m)
 {
-    return (size_t)m * m * 2 + 3 * (size_t)m + 64;     // Aw (m x m), d, e, tau, Zt (m x m)
+    return (size_t)m * m * 7 + 3 * (size_t)m + 128;
 }
 
 // Householder reduction of the full symmetric H (lower reflectors, LAPACK dsytd2 "L").
@@ -805,10 +811,17 @@ __device__ __forceinline__ int sturm_count(int m, const double *d, const double 
     return cnt;
 }
 
-// one warp per wanted eigenvalue index j (il-1+warp), 32-point multisection
+// one warp per wanted eigenvalue index j (il-1+warp), 32-point multisection.
+// guess (may be NULL): an estimate of each wanted eigenvalue (the previous
+// Rayleigh-Ritz step's). Its first round counts at g -/+ |g| 2^-(3l+1), l = 0..15
+// (lanes 0-15 below, 16-31 above); the closest points whose counts still bracket
+// eigenvalue j become the interval, and the multisection goes on from there: a
+// guess within relative d of the eigenvalue leaves a bracket of relative width
+// ~16 d instead of the Gershgorin interval. The counts are monotone in x, so a
+// wrong guess only loses that round.
 __global__ void __launch_bounds__(256)
 k_bisect(int m, const double *__restrict__ dg, const double *__restrict__ eg, int il, int iu,
-         double *__restrict__ eval, int *info)
+         double *__restrict__ eval, int *info, const double *__restrict__ guess)
 {
     extern __shared__ double sm[];
     double *d = sm, *e2 = sm + m;
@@ -839,6 +852,25 @@ k_bisect(int m, const double *__restrict__ dg, const double *__restrict__ eg, in
     if (j > iu) return;                                                // warp-uniform
     double lo = s_gl, hi = s_gu;
     const double piv = s_piv;
+    if (guess) {
+        const double g = guess[j - il];
+        if (isfinite(g) && g != 0.0) {
+            const int l = lane & 15;
+            const double del = ldexp(fabs(g), -(3 * l + 1));
+            const double x = lane < 16 ? g - del : g + del;
+            const int c = sturm_count(m, d, e2, x, piv);
+            const unsigned below = __ballot_sync(FULL, lane < 16 && c < j) & 0xffffu;
+            const unsigned above = __ballot_sync(FULL, lane >= 16 && c >= j) >> 16;
+            if (below) {
+                const double xl = __shfl_sync(FULL, x, 31 - __clz(below));
+                if (xl > lo) lo = xl;
+            }
+            if (above) {
+                const double xh = __shfl_sync(FULL, x, 16 + (31 - __clz(above)));
+                if (xh < hi) hi = xh;
+            }
+        }
+    }
     for (int it = 0; it < 80; ++it) {
         const double width = hi - lo;
         const double tolv = 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + piv;
@@ -1118,8 +1150,66 @@ __global__ void k_check_finite(int m, int nev, const double *Z, int ldz, int *in
         if (!isfinite(Z[(t % m) + (t / m) * (long)ldz])) atomicExch(info, 2);
 }
 
+// Reorthogonalisation of many inverse-iteration vectors by Cholesky-QR.
+// k_cluster_orth orthogonalises each vector against the earlier members of its
+// cluster (eigenvalues closer than 1e-3 ||T||, dstein's criterion) by modified
+// Gram-Schmidt in one thread block; when ||T|| is large against the wanted
+// eigenvalues (a graph pencil: projected spectrum to ~2e3, wanted ones below 1)
+// every wanted vector falls in one cluster, and that block does O(nev^2 m) FP64
+// work alone. Gram-Schmidt over all vectors in index order is the Q factor of
+// Z = Q R, which Cholesky-QR computes with parallel small GEMMs: G = Z^T Z,
+// R^T R = G, Z <- Z R^-1. Inverse-iteration vectors are nearly orthonormal, so
+// one pass leaves them orthonormal to rounding when every pivot keeps at least
+// half of its column's norm squared (condition number of Z below ~1.5); a second
+// pass repairs the first one's rounding otherwise. Vectors of well-separated
+// eigenvalues are already orthogonal to O(eps ||T|| / gap), so the mixing
+// outside the clusters is of that order. A pivot below 1e-10 of its column's
+// norm (nearly dependent vectors) keeps the vectors as they were and the caller
+// falls back to k_cluster_orth. (m = 720, nev = 208, one GB300: 33 ms per
+// dsyevx-signature call against 44.5 ms with k_cluster_orth, both passes run.)
+#define CQ_MIN_NEV 96
+static int cholqr_reorth(gcge_gpu_ctx *ctx, int m, int nev, double *Zt, double *ext, int *done)
+{
+    double *Zq = ext, *G = Zq + (size_t)m * m, *Tq = G + (size_t)m * m, *cw = Tq + (size_t)m * m;
+    double *ratio_dev = cw + 2 * (size_t)m * m;
+    int *kept_dev = (int *)(ratio_dev + 8);
+    *done = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        double *src = pass == 0 ? Zt : Zq, *dst = pass == 0 ? Zq : Zt;
+        int st = gb_small_gemm(ctx, 'T', 'N', nev, nev, m, 1.0, src, m, src, m, 0.0, G, nev);
+        if (st) return st;
+        GB_LAUNCH(ctx, k_chol_deflate, 1, 512, 2 * nev * sizeof(int), nev, G, nev, Tq, kept_dev, 0.0, 1e-10, cw,
+                  cw + (size_t)nev * nev, ratio_dev);
+        struct { int kept; int pad; double ratio; } h = {0, 0, 0.0};
+        if (cudaMemcpyAsync(&h.kept, kept_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+            cudaMemcpyAsync(&h.ratio, ratio_dev, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+            cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+            return gb_fail(ctx, GCGE_GPU_ERR_CUDA);
+        if (h.kept != nev) {
+            // nearly dependent vectors: leave them (the second pass' input is copied back)
+            if (pass == 1 && (st = gb_copy_block(ctx, m, nev, Zq, m, Zt, m))) return st;
+            return GCGE_GPU_OK;
+        }
+        if ((st = gb_small_gemm(ctx, 'N', 'N', m, nev, nev, 1.0, src, m, Tq, nev, 0.0, dst, m))) return st;
+        if (pass == 0 && h.ratio >= 0.5) {
+            if ((st = gb_copy_block(ctx, m, nev, Zq, m, Zt, m))) return st;
+            break;
+        }
+    }
+    *done = 1;
+    return GCGE_GPU_OK;
+}
+
+extern "C" int gb_syevx_guess(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int il, int iu, double *eval,
+                              double *Z, int ldz, double *work, int *info_dev, const double *guess);
 extern "C" int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int il, int iu, double *eval,
                         double *Z, int ldz, double *work, int *info_dev)
+{
+    return gb_syevx_guess(ctx, m, H, ldh, il, iu, eval, Z, ldz, work, info_dev, nullptr);
+}
+
+extern "C" int gb_syevx_guess(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int il, int iu, double *eval,
+                              double *Z, int ldz, double *work, int *info_dev, const double *guess)
 {
     if (m <= 0 || il < 1 || iu > m || il > iu) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     if (m > 3000) return gb_fail(ctx, GCGE_GPU_ERR_ARG);   // dynamic shared memory of k_tridiag / k_bisect (2m doubles)
@@ -1148,7 +1238,7 @@ extern "C" int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int 
     const int warps_per_block = 1;     // one eigenvalue per SM: the Sturm chains use the FP64 pipe
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
     GB_LAUNCH(ctx, k_bisect, (nev + warps_per_block - 1) / warps_per_block, 32 * warps_per_block,
-              2 * m * sizeof(double), m, d, e, il, iu, eval, info_dev);
+              2 * m * sizeof(double), m, d, e, il, iu, eval, info_dev, guess);
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
     // inverse iteration: one eigenvalue per one-warp block, so that the chains spread
     // over the SMs (the FP64 pipe of an SM is narrow: chains sharing one SM queue
@@ -1169,8 +1259,15 @@ extern "C" int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int 
     }
     GB_LAUNCH(ctx, k_invit, (nev + IV - 1) / IV, 32, ismem, m, d, e, nev, eval, Zt, m, IV);
     GB_PROF(ctx, GB_K_EIG, 0.0, 0.0);
+    int reorth_done = 0;
+    if (nev >= CQ_MIN_NEV) {
+        const int st = cholqr_reorth(ctx, m, nev, Zt, Zt + (size_t)m * m, &reorth_done);
+        if (st) return st;
+    }
     const size_t osmem = sizeof(double) * (size_t)m * nev;
-    if (osmem <= 160 * 1024) {
+    if (reorth_done) {
+        // the vectors are orthonormal: Cholesky-QR over all of them
+    } else if (osmem <= 160 * 1024) {
         GB_LAUNCH(ctx, k_cluster_orth<true>, 1, 1024, osmem, m, d, e, nev, eval, Zt, m);
     } else {
         GB_LAUNCH(ctx, k_cluster_orth<false>, 1, 1024, 0, m, d, e, nev, eval, Zt, m);

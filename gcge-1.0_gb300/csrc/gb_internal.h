@@ -205,6 +205,11 @@ int gb_chol_deflate(gcge_gpu_ctx *ctx, int k, const double *G, int ldg, double *
 size_t gb_syevx_work_doubles(int m);
 int gb_syevx(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int il, int iu, double *eval,
              double *Z, int ldz, double *work, int *info_dev);
+/* the same with an estimate of each wanted eigenvalue (device array of iu-il+1
+ * values, the previous Rayleigh-Ritz step's; may alias eval) that narrows the
+ * bisection's starting intervals */
+int gb_syevx_guess(gcge_gpu_ctx *ctx, int m, const double *H, int ldh, int il, int iu, double *eval, double *Z,
+                   int ldz, double *work, int *info_dev, const double *guess);
 /* small helpers used by the solver */
 int gb_set_zero(gcge_gpu_ctx *ctx, double *a, size_t count);
 int gb_copy_d(gcge_gpu_ctx *ctx, double *dst, const double *src, size_t count);

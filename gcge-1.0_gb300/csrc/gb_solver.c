@@ -213,13 +213,17 @@ static int rr_eig_solve(gcg_t *g)
         if (sl >= iu) sl = 0;
     }
     g->soft_locked = sl;
-    if (sl == 0) return gb_syevx(g->ctx, ldm, g->H, ldm, 1, iu, g->eval_d, g->C, ldm, g->eig_work, g->info_d);
+    /* the previous step's eigenvalues of the projected matrix start the bisection
+     * (lambda, or nu in A-orthogonal mode; zeros before the first step) */
+    const double *guess = g->amode ? g->nu_d : g->eval_d;
+    if (sl == 0)
+        return gb_syevx_guess(g->ctx, ldm, g->H, ldm, 1, iu, g->eval_d, g->C, ldm, g->eig_work, g->info_d, guess);
     /* the locked pairs keep their eigenvalues and are the unit vectors of the
      * projected basis; only the trailing (ldm - sl) block is solved */
     int st = gb_soft_lock(g->ctx, g->H, ldm, ldm, g->dim_xp, sl, g->C, ldm, iu);
     if (st) return st;
-    return gb_syevx(g->ctx, ldm - sl, g->H + (size_t)sl * ldm + sl, ldm, 1, iu - sl, g->eval_d + sl,
-                    g->C + (size_t)sl * ldm + sl, ldm, g->eig_work, g->info_d);
+    return gb_syevx_guess(g->ctx, ldm - sl, g->H + (size_t)sl * ldm + sl, ldm, 1, iu - sl, g->eval_d + sl,
+                          g->C + (size_t)sl * ldm + sl, ldm, g->eig_work, g->info_d, guess + sl);
 }
 
 /* GCGE_ComputeX (src/gcge_xpw.c:47-76): X[:, s:nev] = V[:, s:dim_xpw] C[s:, s:nev], s
