@@ -1,5 +1,6 @@
 // gb_api.cu -- C ABI: context, device CSR matrices, multivectors, block
 // operations and the Cholesky-QR orthonormalisation (include/gcge_gb300.h).
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -394,6 +395,41 @@ __global__ void k_csr_check(int n, int nnz, const int *__restrict__ rp, const in
     }
 }
 
+// Rows with more than GB_LONG_ROW entries, longest first (ties by row), listed
+// for the FP32 block-CG SpMM, which gives each of them a whole block (a
+// grid-stride row split would leave a power-law graph's hub rows, up to
+// thousands of entries, to one lane group). Called after the structure check,
+// so the lengths are valid.
+static int gb_list_long_rows(gcge_gpu_ctx *ctx, gcge_gpu_mat *A, const int *rowptr)
+{
+    long cnt = 0, nz = 0;
+    for (int r = 0; r < A->n; ++r)
+        if (rowptr[r + 1] - rowptr[r] > GB_LONG_ROW) ++cnt;
+    if (!cnt) return 0;
+    int *h = (int *)malloc(sizeof(int) * cnt);
+    if (!h) return 1;
+    cnt = 0;
+    for (int r = 0; r < A->n; ++r) {
+        const int len = rowptr[r + 1] - rowptr[r];
+        if (len > GB_LONG_ROW) {
+            h[cnt++] = r;
+            nz += len;
+        }
+    }
+    std::sort(h, h + cnt, [rowptr](int a, int b) {
+        const int la = rowptr[a + 1] - rowptr[a], lb = rowptr[b + 1] - rowptr[b];
+        return la != lb ? la > lb : a < b;
+    });
+    int rc = cudaMalloc(&A->lrows, sizeof(int) * cnt) != cudaSuccess ||
+             cudaMemcpyAsync(A->lrows, h, sizeof(int) * cnt, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+             cudaStreamSynchronize(ctx->stream) != cudaSuccess;
+    free(h);
+    if (rc) return 1;
+    A->nlong = (int)cnt;
+    A->nnz_long = nz;
+    return 0;
+}
+
 // The structure is checked on the device after the upload (a host loop over
 // the column indices cost ~20 ms per 40 M entries, on the path of every
 // host-buffer solve); the result is read back with the creation's final sync.
@@ -447,6 +483,10 @@ extern "C" int GCGE_GPU_MatCreate(gcge_gpu_ctx *ctx, int n, const int *rowptr, c
         return gb_fail(ctx, GCGE_GPU_ERR_CSR);
     }
     A->max_row_nnz = h[1];
+    if (keep_fp32 && h[1] > GB_LONG_ROW && gb_list_long_rows(ctx, A, rowptr)) {
+        GCGE_GPU_MatDestroy(A);
+        return gb_fail(ctx, GCGE_GPU_ERR_NOMEM);
+    }
     *out = A;
     return GCGE_GPU_OK;
 }
@@ -489,6 +529,7 @@ extern "C" int GCGE_GPU_MatDestroy(gcge_gpu_mat *A)
     if (A->dinv32) cudaFree(A->dinv32);
     if (A->vpair) cudaFree(A->vpair);
     if (A->pair_meta) cudaFree(A->pair_meta);
+    if (A->lrows) cudaFree(A->lrows);
     free(A);
     return GCGE_GPU_OK;
 }

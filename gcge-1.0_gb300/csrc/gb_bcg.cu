@@ -217,11 +217,15 @@ static int row_grid(gcge_gpu_ctx *ctx, long rows)
     return (int)g;
 }
 
+// partial-sum rows kept for the blocks of the FP32 long-row SpMM (past the
+// cdiv(n, RED_ROWS) rows of the other kernels)
+#define LONG_PART_ROWS 2048
+
 extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
 {
     long ldk = (k + 3) & ~3;   // 16-byte rows for the vectorised SpMM
     size_t vec = precision ? sizeof(float) : sizeof(double);
-    size_t nblk = (size_t)cdiv(n > 0 ? n : 1, RED_ROWS);
+    size_t nblk = (size_t)cdiv(n > 0 ? n : 1, RED_ROWS) + (precision ? LONG_PART_ROWS : 0);
     size_t blocks = 4 * (size_t)n * ldk * vec;  // R, X, P, W
     size_t state = (7 * (size_t)k + nblk * (size_t)k + 8) * sizeof(double) + 64;
     return blocks + state + 16 * 256;   // every sub-buffer is aligned to 256 bytes (10 of them)
@@ -371,19 +375,89 @@ k_xr_update_v(int n, int k, float *__restrict__ X, float *__restrict__ R, const 
     vb_block_reduce<RPB, 4 * TPR>(s, rs, cg, blockIdx.y * 64, ka, k, part);
 }
 
+// The long rows (the list lrows, nlong of them, longest first: a power-law
+// graph's hubs reach thousands of entries) of W = A P: each block takes one row
+// at a time with all 256 / L lane groups, group g summing the row's entries
+// g L .. + L - 1 modulo 256, and the group sums are added in shared memory in
+// group order. Rows are dealt to the blocks in snake order (round r: block b
+// takes list entry r G + b, or r G + G - 1 - b for odd r), so the blocks carry
+// nearly equal entry counts. Column c's p.w partial is summed in FP64 by thread
+// c and written to row part_row0 + blockIdx.x of part.
+template <int L, int NV>
+__global__ void __launch_bounds__(VB_THREADS)
+k_spmm32_long(const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+              const float *__restrict__ P, float *__restrict__ W, long ld, int k, const int *__restrict__ nact,
+              double *__restrict__ part, int part_row0, const int *__restrict__ lrows, int nlong)
+{
+    constexpr int RPB = VB_THREADS / L, COLS = 4 * L * NV, UNR = NV == 1 ? 4 : 2;
+    __shared__ float rs[RPB * COLS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / L, sl = lane % L;
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (sub * L));
+    const int slot = warp * (32 / L) + sub;
+    const int kact = min(*nact, k), G = gridDim.x, b = blockIdx.x;
+    double pw = 0.0;
+    for (int r = 0; kact > 0; ++r) {
+        const long li = (long)r * G + ((r & 1) ? G - 1 - b : b);
+        if (li >= nlong) break;
+        const long row = lrows[li];
+        const int beg = rp[row], end = rp[row + 1];
+        float acc[4 * NV];
+#pragma unroll
+        for (int q = 0; q < 4 * NV; ++q) acc[q] = 0.f;
+        for (int base = beg + slot * L; base < end; base += RPB * L) {
+            const int e = base + sl;
+            int j = 0;
+            float a = 0.f;
+            if (e < end) { j = __ldg(ci + e); a = __ldg(val + e); }
+            const int m = min(L, end - base);
+#pragma unroll UNR
+            for (int t = 0; t < m; ++t) {
+                const int jj = __shfl_sync(gmask, j, t, L);
+                const float aa = __shfl_sync(gmask, a, t, L);
+                const float *xr = P + (long)jj * ld + 4 * sl;
+#pragma unroll
+                for (int v = 0; v < NV; ++v)
+                    if (4 * sl + 4 * L * v < kact) {
+                        const float4 xv = __ldg(reinterpret_cast<const float4 *>(xr + 4 * L * v));
+                        acc[4 * v + 0] = fmaf(aa, xv.x, acc[4 * v + 0]);
+                        acc[4 * v + 1] = fmaf(aa, xv.y, acc[4 * v + 1]);
+                        acc[4 * v + 2] = fmaf(aa, xv.z, acc[4 * v + 2]);
+                        acc[4 * v + 3] = fmaf(aa, xv.w, acc[4 * v + 3]);
+                    }
+            }
+        }
+        __syncthreads();                                      // the previous row's sums are read
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) rs[slot * COLS + 4 * sl + 4 * L * v + q] = acc[4 * v + q];
+        __syncthreads();
+        const int c = threadIdx.x;
+        if (c < COLS && c < kact) {
+            float t = 0.f;
+            for (int g = 0; g < RPB; ++g) t += rs[g * COLS + c];
+            W[row * ld + c] = t;
+            pw += (double)(P[row * ld + c] * t);
+        }
+    }
+    if (threadIdx.x < COLS && (int)threadIdx.x < kact) part[(long)(part_row0 + b) * k + threadIdx.x] = pw;
+}
+
 // W = A P (FP32, the first nact columns) and block partials of p.w: L lanes per
 // row, NV float4 column groups per lane (lane l owns columns 4l + 4Lv .. +3, so
 // that each group load of the L lanes reads one contiguous 16L-byte run), 256 / L
 // rows per block pass; grid-stride over rows (measured faster than contiguous row
-// ranges per block on the Q1 cube). NV = 2 halves the shuffles and address
-// arithmetic per FMA. The p.w products are summed in FP32 over runs of 8 rows of
-// a row slot and the runs added in FP64 to the slot's shared-memory partials
-// (the thread's own entries: no atomics, fixed order).
+// ranges per block on the Q1 cube). Rows longer than lim are skipped (the long-row
+// kernel above has them). NV = 2 halves the shuffles and address arithmetic per
+// FMA. The p.w products are summed in FP32 over runs of 8 rows of a row slot and
+// the runs added in FP64 to the slot's shared-memory partials (the thread's own
+// entries: no atomics, fixed order).
 template <int L, int NV>
 __global__ void __launch_bounds__(VB_THREADS, 5)                  // 48 registers: 5 blocks per SM
 k_spmm32_dot(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
              const float *__restrict__ P, float *__restrict__ W, long ld, int k, const int *__restrict__ nact,
-             double *__restrict__ part)
+             double *__restrict__ part, int lim)
 {
     constexpr int RPB = VB_THREADS / L, COLS = 4 * L * NV, UNR = NV == 1 ? 4 : 2;
     __shared__ double red[RPB][COLS + 1];
@@ -403,6 +477,7 @@ k_spmm32_dot(int n, const int *__restrict__ rp, const int *__restrict__ ci, cons
     if (kact > 0)
         for (long row = (long)blockIdx.x * RPB + slot; row < n; row += (long)gridDim.x * RPB) {
             const int beg = rp[row], end = rp[row + 1];
+            if (end - beg > lim) continue;                    // a long row: k_spmm32_long
             float acc[4 * NV];
 #pragma unroll
             for (int q = 0; q < 4 * NV; ++q) acc[q] = 0.f;
@@ -530,7 +605,9 @@ k_colsum_finalize(int nblk, int k, const double *__restrict__ part, double *sums
 typedef void (*pupdate_fn)(int, int, const float *, float *, long, const double *, const int *, int,
                            const float *);
 typedef void (*spmm32_fn)(int, const int *, const int *, const float *, const float *, float *, long, int,
-                          const int *, double *);
+                          const int *, double *, int);
+typedef void (*spmm32l_fn)(const int *, const int *, const float *, const float *, float *, long, int, const int *,
+                           double *, int, const int *, int);
 typedef void (*xr_fn)(int, int, float *, float *, const float *, const float *, long, const double *, const int *,
                       double *, const float *);
 
@@ -538,7 +615,7 @@ static int bcg_rounds32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, float *R, floa
                         const gb_bcg_args *a, bcg_state *s)
 {
     const int n = a->n, k = a->k;
-    if (k > 128 || !A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
+    if (k > 256 || !A->v32) return gb_fail(ctx, GCGE_GPU_ERR_ARG);
     const int ctiles = (k + 63) / 64;
     // vector kernels: threads per row whose float4 groups cover k; SpMM: L lanes per
     // row with NV float4 groups each, 4 L NV >= k
@@ -548,17 +625,44 @@ static int bcg_rounds32(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, float *R, floa
     const xr_fn xru = tpr == 1 ? k_xr_update_v<1> : tpr == 2 ? k_xr_update_v<2> : tpr == 4 ? k_xr_update_v<4>
                     : tpr == 8 ? k_xr_update_v<8> : k_xr_update_v<16>;
     const spmm32_fn spm = k <= 4 ? k_spmm32_dot<1, 1> : k <= 8 ? k_spmm32_dot<2, 1> : k <= 16 ? k_spmm32_dot<4, 1>
-                        : k <= 32 ? k_spmm32_dot<4, 2> : k <= 64 ? k_spmm32_dot<8, 2> : k_spmm32_dot<16, 2>;
+                        : k <= 32 ? k_spmm32_dot<4, 2> : k <= 64 ? k_spmm32_dot<8, 2>
+                        : k <= 128 ? k_spmm32_dot<16, 2> : k_spmm32_dot<32, 2>;
     const int Gp = vec_blocks(ctx, (const void *)pup, n, ctiles);
     const int Gs = vec_blocks(ctx, (const void *)spm, n, 1);
     const int Gx = vec_blocks(ctx, (const void *)xru, n, ctiles);
+    // rows longer than GB_LONG_ROW: a launch of their own before the grid-stride
+    // product (one wave of blocks over the sorted list); its p.w partials follow
+    // the Gs rows of the other launch in part, which holds LONG_PART_ROWS rows
+    // past cdiv(n, RED_ROWS)
+    const spmm32l_fn spl = k <= 4 ? k_spmm32_long<1, 1> : k <= 8 ? k_spmm32_long<2, 1> : k <= 16 ? k_spmm32_long<4, 1>
+                         : k <= 32 ? k_spmm32_long<4, 2> : k <= 64 ? k_spmm32_long<8, 2>
+                         : k <= 128 ? k_spmm32_long<16, 2> : k_spmm32_long<32, 2>;
+    int Gl = 0;
+    if (A->nlong > 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)spl, VB_THREADS, 0) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        const long room = cdiv(n, RED_ROWS) + LONG_PART_ROWS - (long)Gs, cap = (long)ctx->num_sms * per_sm;
+        long g = A->nlong < cap ? A->nlong : cap;
+        Gl = (int)(g < room ? g : room);
+        if (Gl < 0) Gl = 0;
+    }
+    const int lim = Gl > 0 ? GB_LONG_ROW : 0x7fffffff;
+    const double lbytes = Gl > 0 ? 8.0 * A->nnz_long + 12.0 * A->nlong * k : 0.0;
     for (int it = 1; it < a->max_it; ++it) {
         GB_PROF(ctx, GB_K_BCGVEC, 12.0 * n * k, 2.0 * n * k);
         GB_LAUNCH(ctx, pup, dim3(Gp, ctiles), VB_THREADS, 0, n, k, R, P, ld, s->beta, s->nact, it == 1, a->dinv32);
         ctx->spmm_launches++;
-        GB_PROF(ctx, GB_K_SPMM32, 8.0 * A->nnz + 4.0 * (A->n + 1) + 12.0 * A->n * k, 2.0 * A->nnz * k + 2.0 * A->n * k);
-        GB_LAUNCH(ctx, spm, Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part);
-        GB_LAUNCH(ctx, k_colsum_alpha, k, 256, 0, Gs, k, s->part, s->nact, s->rho2, s->ptw, s->alpha);
+        if (Gl > 0) {
+            GB_PROF(ctx, GB_K_SPMM32, lbytes, 2.0 * A->nnz_long * k + 2.0 * A->nlong * k);
+            GB_LAUNCH(ctx, spl, Gl, VB_THREADS, 0, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part, Gs, A->lrows,
+                      A->nlong);
+        }
+        GB_PROF(ctx, GB_K_SPMM32, 8.0 * A->nnz + 4.0 * (A->n + 1) + 12.0 * A->n * k - lbytes,
+                2.0 * (A->nnz - (Gl > 0 ? A->nnz_long : 0)) * k + 2.0 * A->n * k);
+        GB_LAUNCH(ctx, spm, Gs, VB_THREADS, 0, n, A->rp, A->ci, A->v32, P, W, ld, k, s->nact, s->part, lim);
+        GB_LAUNCH(ctx, k_colsum_alpha, k, 256, 0, Gs + Gl, k, s->part, s->nact, s->rho2, s->ptw, s->alpha);
         GB_PROF(ctx, GB_K_BCGVEC, 24.0 * n * k, 6.0 * n * k);
         GB_LAUNCH(ctx, xru, dim3(Gx, ctiles), VB_THREADS, 0, n, k, X, R, P, W, ld, s->alpha, s->nact, s->part,
                   a->dinv32);
@@ -617,7 +721,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     s.alpha = (double *)take(sizeof(double) * k);
     s.beta = (double *)take(sizeof(double) * k);
     s.sums = (double *)take(sizeof(double) * k);
-    s.part = (double *)take(sizeof(double) * (size_t)nblk * k);
+    s.part = (double *)take(sizeof(double) * (size_t)(nblk + (a->precision ? LONG_PART_ROWS : 0)) * k);
     s.nact = (int *)take(64);
     dim3 rgrid(nblk, (k + 31) / 32);
     if (a->precision == 0) {
@@ -665,7 +769,7 @@ extern "C" int gb_bcg(gcge_gpu_ctx *ctx, const gcge_gpu_mat *A, double *RHS, lon
     GB_LAUNCH(ctx, k_dot_partial<float>, rgrid, 256, 0, n, k, R, R, ld, (const int *)nullptr, s.part, a->dinv32);
     GB_LAUNCH(ctx, k_colsum, k, 256, 0, nblk, k, s.part, (const int *)nullptr, s.sums);
     GB_LAUNCH(ctx, k_init_state, 1, 256, 0, k, s.sums, s.rho2, s.err, s.nact);
-    if ((st = k <= 128 ? bcg_rounds32(ctx, A, R, D, P, W, ld, a, &s) : bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s)))
+    if ((st = k <= 256 ? bcg_rounds32(ctx, A, R, D, P, W, ld, a, &s) : bcg_rounds<float>(ctx, A, R, D, P, W, ld, a, &s)))
         return st;
     GB_LAUNCH(ctx, k_add_f2d, row_grid(ctx, n), 256, 0, n, k, D, ld, X, ldx);
     return a->residual_unused ? GCGE_GPU_OK : gb_convert_f2d(ctx, n, k, R, ld, RHS, ldr);

@@ -85,7 +85,13 @@ struct gcge_gpu_mat {
     float *dinv32;             /* the same in FP32 */
     float *vpair;              /* values x 2^-s as (hi, lo) FP32 pairs (lazy) or NULL */
     int *pair_meta;            /* device: [0..1] max |value| bits, [2] the exponent s */
+    int *lrows;                /* device: rows with more than GB_LONG_ROW entries (FP32 matrices) */
+    int nlong;                 /* their count */
+    long nnz_long;             /* their entries */
 };
+
+/* rows longer than this are shared by a whole block in the FP32 block-CG SpMM */
+#define GB_LONG_ROW 64
 
 struct gcge_gpu_mv {
     gcge_gpu_ctx *ctx;

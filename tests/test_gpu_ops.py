@@ -165,6 +165,29 @@ def test_bcg_fp32_tracks_fp64_while_columns_deactivate(ctx, k, max_it, rate):
     assert rel(out[1], out[0]) < 1e-4
 
 
+@pytest.mark.parametrize("k", [3, 8, 16, 30, 64, 100, 200])
+def test_bcg_fp32_long_rows(ctx, k):
+    """A power-law graph whose hub rows exceed the long-row length: those rows go
+    to the block-per-row SpMM launch, the rest to the grid-stride one; the FP32
+    iterate tracks the FP64 one and repeats bit for bit (fixed-order sums). The
+    shift keeps the condition number near 25, so that FP32 rounding, amplified by
+    the rounds roughly in proportion to it, stays far below the bound, while a
+    wrong sum over a hub row would not."""
+    A, _ = P.powerlaw_graph(n=20000, seed=11, shift=100.0)
+    assert int(np.sum(np.diff(A.rowptr) > 64)) > 100
+    rng = np.random.default_rng(200 + k)
+    R0 = rng.standard_normal((A.n, k))
+    dA = ctx.matrix(A, keep_fp32=True)
+    out = []
+    for prec in (0, 1, 1):
+        r, w = ctx.multivec(A.n, k, R0), ctx.multivec(A.n, k)
+        G.bcg(dA, r, 0, w, 0, k, cg_max_it=12, cg_rate=1e-30, precision=prec)
+        out.append(w.download())
+    assert np.all(np.isfinite(out[1]))
+    assert rel(out[1], out[0]) < 1e-4
+    assert np.array_equal(out[1], out[2])
+
+
 def test_newton_reciprocal_of_inverse_iteration(ctx):
     """The reciprocal used for the pivots of inverse iteration (hardware
     approximation refined by two Newton-Raphson steps) is within 2 ulp of the
