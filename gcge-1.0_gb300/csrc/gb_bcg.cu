@@ -389,7 +389,7 @@ k_spmm32_long(const int *__restrict__ rp, const int *__restrict__ ci, const floa
               const float *__restrict__ P, float *__restrict__ W, long ld, int k, const int *__restrict__ nact,
               double *__restrict__ part, int part_row0, const int *__restrict__ lrows, int nlong)
 {
-    constexpr int RPB = VB_THREADS / L, COLS = 4 * L * NV, UNR = NV == 1 ? 4 : 2;
+    constexpr int RPB = VB_THREADS / L, COLS = 4 * L * NV, UNR = 4;
     __shared__ float rs[RPB * COLS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / L, sl = lane % L;
@@ -450,16 +450,19 @@ k_spmm32_long(const int *__restrict__ rp, const int *__restrict__ ci, const floa
 // rows per block pass; grid-stride over rows (measured faster than contiguous row
 // ranges per block on the Q1 cube). Rows longer than lim are skipped (the long-row
 // kernel above has them). NV = 2 halves the shuffles and address arithmetic per
-// FMA. The p.w products are summed in FP32 over runs of 8 rows of a row slot and
-// the runs added in FP64 to the slot's shared-memory partials (the thread's own
-// entries: no atomics, fixed order).
+// FMA. The gathers of P rows are L2 hits whose latency bounds the kernel, so four
+// entries' loads are in flight per lane (64 registers, 4 blocks per SM: 8% faster
+// at fem96 k = 64 than two at 48 registers and 5 blocks). The p.w products are
+// summed in FP32 over runs of 8 rows of a row slot and the runs added in FP64 to
+// the slot's shared-memory partials (the thread's own entries: no atomics, fixed
+// order).
 template <int L, int NV>
-__global__ void __launch_bounds__(VB_THREADS, 5)                  // 48 registers: 5 blocks per SM
+__global__ void __launch_bounds__(VB_THREADS, 4)                  // 64 registers: 4 blocks per SM
 k_spmm32_dot(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
              const float *__restrict__ P, float *__restrict__ W, long ld, int k, const int *__restrict__ nact,
              double *__restrict__ part, int lim)
 {
-    constexpr int RPB = VB_THREADS / L, COLS = 4 * L * NV, UNR = NV == 1 ? 4 : 2;
+    constexpr int RPB = VB_THREADS / L, COLS = 4 * L * NV, UNR = 4;
     __shared__ double red[RPB][COLS + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int sub = lane / L, sl = lane % L;

@@ -188,6 +188,30 @@ def test_bcg_fp32_long_rows(ctx, k):
     assert np.array_equal(out[1], out[2])
 
 
+@pytest.mark.parametrize("k", [33, 40, 64])
+def test_bcg_fp32_fem_cube(ctx, k):
+    """Q1 cube stiffness (27 entries per row) at the solver's block widths: the
+    FP32 iterate tracks the FP64 one and repeats bit for bit; new values of the
+    same structure scale the result exactly (2 A: half the iterate)."""
+    A, _ = P.fem_q1_cube(24)
+    rng = np.random.default_rng(300 + k)
+    R0 = rng.standard_normal((A.n, k))
+    dA = ctx.matrix(A, keep_fp32=True)
+    out = []
+    for prec in (0, 1, 1):
+        r, w = ctx.multivec(A.n, k, R0), ctx.multivec(A.n, k)
+        G.bcg(dA, r, 0, w, 0, k, cg_max_it=12, cg_rate=1e-30, precision=prec)
+        out.append(w.download())
+    assert np.all(np.isfinite(out[1]))
+    assert rel(out[1], out[0]) < 1e-4
+    assert np.array_equal(out[1], out[2])
+    # new values, same structure: 2 A
+    dA.set_values(2.0 * A.val)
+    r, w = ctx.multivec(A.n, k, R0), ctx.multivec(A.n, k)
+    G.bcg(dA, r, 0, w, 0, k, cg_max_it=12, cg_rate=1e-30, precision=1)
+    assert rel(2.0 * w.download(), out[1]) < 1e-5
+
+
 def test_newton_reciprocal_of_inverse_iteration(ctx):
     """The reciprocal used for the pivots of inverse iteration (hardware
     approximation refined by two Newton-Raphson steps) is within 2 ulp of the
