@@ -522,6 +522,22 @@ k_tridiag_smem(int m, const double *__restrict__ H, int ldh, double *__restrict_
         for (int r = c + lane; r < m; r += 32) Aw[r + (long)c * m] = L[off(c) + (r - c)];
 }
 
+// 1/x by Newton-Raphson refinement of the hardware reciprocal approximation
+// (rcp.approx.ftz.f64): two steps r <- r + r (1 - x r) square the relative error
+// each time, leaving a few ulp. For the pivots of inverse iteration, whose
+// iterate tolerates a slightly perturbed solve; an exact IEEE division costs
+// several hundred cycles on this chain. Tiny or zero x take the exact division.
+__device__ __forceinline__ double nr_recip(double x)
+{
+    if (!(fabs(x) >= DBL_MIN) || isinf(x)) return 1.0 / x;
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double t = fma(-x, r, 1.0);
+    r = fma(r, t, r);
+    t = fma(-x, r, 1.0);
+    return fma(r, t, r);
+}
+
 // ---------------------------------------------------------------- cluster tridiagonalisation
 // The same reduction as k_tridiag (dsytd2 "L": reflectors in the columns of Aw,
 // d, e, tau) spread over a thread-block cluster of TC CTAs, so that the FP64 work
@@ -608,9 +624,11 @@ k_tridiag_cluster(int m, const double *__restrict__ H, int ldh, double *__restri
                     e[i] = alpha;
                     s_scale = 0.0;
                 } else {
+                    // the two quotients by Newton reciprocals (a few ulp): an IEEE
+                    // division is several hundred cycles on this serial path
                     const double beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-                    s_tau = (beta - alpha) / beta;
-                    s_scale = 1.0 / (alpha - beta);
+                    s_tau = (beta - alpha) * nr_recip(beta);
+                    s_scale = nr_recip(alpha - beta);
                     e[i] = beta;
                 }
                 tau[i] = s_tau;
@@ -666,8 +684,14 @@ k_tridiag_cluster(int m, const double *__restrict__ H, int ldh, double *__restri
         // ---- C: p = tau * sum of the partials (rank order), K, w, rank-2 update
         if (tv != 0.0) {
             for (int r = tid; r < len; r += TD_THREADS) {
+                // all TC remote loads issued before the sum (rank order kept)
+                double t[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) t[q] = q < TC ? cl.map_shared_rank(pbuf + (size_t)par * m, q)[r] : 0.0;
                 double s = 0;
-                for (int q = 0; q < TC; ++q) s += cl.map_shared_rank(pbuf + (size_t)par * m, q)[r];
+#pragma unroll
+                for (int q = 0; q < 16; ++q)
+                    if (q < TC) s += t[q];
                 p[r] = tv * s;
             }
             __syncthreads();
@@ -718,15 +742,18 @@ static size_t td_cluster_smem(int m, int tc)
 }
 
 // cluster size for m, 0 if the single-SM kernel is to be used
-// Each of the m - 2 steps carries several microseconds of dependent FP64 latency
-// (reductions, the sqrt/division of the reflector, two cluster barriers) whatever
-// the number of SMs, so the cluster pays only where a step's arithmetic on one
-// SM (3 len^2 / 2 FMAs at ~2 FP64 FMA per clock) outweighs that: measured at
-// m = 178 the cluster takes 1.58 ms against 1.47 ms on one SM; m >= 256 goes
-// to the cluster (at m = 720 one SM needs ~60 ms of FP64 issue per reduction).
+// Each of the m - 2 steps carries dependent FP64 latency (reductions, the sqrt
+// and reciprocals of the reflector, two cluster barriers, the gather of the
+// partial products) whatever the number of SMs, so the cluster pays only where
+// a step's arithmetic on one SM (3 len^2 / 2 FMAs at ~2 FP64 FMA per clock)
+// outweighs that. With the partials' remote loads issued together and Newton
+// reciprocals, 16 CTAs win from m = 128 on: the dsyevx-signature call at
+// m = 178 (58 wanted pairs) takes 4.69 ms against 6.45 ms with the single-SM
+// reduction (8 CTAs: 4.93 ms), at m = 130 3.23 against 3.94 ms (at m = 720
+// one SM would need ~60 ms of FP64 issue per reduction).
 static int td_cluster_size(gcge_gpu_ctx *ctx, int m)
 {
-    if (m < 256) return 0;
+    if (m < 128) return 0;
     static int cached_m = -1, cached_tc = 0;
     if (m == cached_m) {
         if (cached_tc &&
@@ -744,7 +771,7 @@ static int td_cluster_size(gcge_gpu_ctx *ctx, int m)
             allow16 = 1;
         cudaGetLastError();
     }
-    const int want = m >= 256 && allow16 ? 16 : 8;
+    const int want = allow16 ? 16 : 8;
     for (int tc = want; tc >= 8; tc /= 2) {
         const size_t smem = td_cluster_smem(m, tc);
         if (smem > 200 * 1024) continue;
@@ -908,22 +935,6 @@ __device__ __forceinline__ double start_value(int j, int i)
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
     z ^= z >> 31;
     return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
-}
-
-// 1/x by Newton-Raphson refinement of the hardware reciprocal approximation
-// (rcp.approx.ftz.f64): two steps r <- r + r (1 - x r) square the relative error
-// each time, leaving a few ulp. For the pivots of inverse iteration, whose
-// iterate tolerates a slightly perturbed solve; an exact IEEE division costs
-// several hundred cycles on this chain. Tiny or zero x take the exact division.
-__device__ __forceinline__ double nr_recip(double x)
-{
-    if (!(fabs(x) >= DBL_MIN) || isinf(x)) return 1.0 / x;
-    double r;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
-    double t = fma(-x, r, 1.0);
-    r = fma(r, t, r);
-    t = fma(-x, r, 1.0);
-    return fma(r, t, r);
 }
 
 __global__ void k_recip_probe(int n, const double *__restrict__ x, double *__restrict__ r)
