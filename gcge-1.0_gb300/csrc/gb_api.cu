@@ -395,31 +395,42 @@ __global__ void k_csr_check(int n, int nnz, const int *__restrict__ rp, const in
     }
 }
 
-// Rows with more than GB_LONG_ROW entries, longest first (ties by row), listed
-// for the FP32 block-CG SpMM, which gives each of them a whole block (a
-// grid-stride row split would leave a power-law graph's hub rows, up to
-// thousands of entries, to one lane group). Called after the structure check,
-// so the lengths are valid.
+// Rows with more than thresh entries, longest first (ties by row), written to
+// out (room for every row); returns their count and their entries in *nnz_long.
+// Host only (internal, not part of the public interface; the CPU tests call it).
+extern "C" int gb_long_rows_host(int n, const int *rowptr, int thresh, int *out, long *nnz_long)
+{
+    int cnt = 0;
+    long nz = 0;
+    for (int r = 0; r < n; ++r) {
+        const int len = rowptr[r + 1] - rowptr[r];
+        if (len > thresh) {
+            out[cnt++] = r;
+            nz += len;
+        }
+    }
+    std::sort(out, out + cnt, [rowptr](int a, int b) {
+        const int la = rowptr[a + 1] - rowptr[a], lb = rowptr[b + 1] - rowptr[b];
+        return la != lb ? la > lb : a < b;
+    });
+    if (nnz_long) *nnz_long = nz;
+    return cnt;
+}
+
+// The rows longer than GB_LONG_ROW, listed on the device for the FP32 block-CG
+// SpMM, which gives each of them a whole block (a grid-stride row split would
+// leave a power-law graph's hub rows, up to thousands of entries, to one lane
+// group). Called after the structure check, so the lengths are valid.
 static int gb_list_long_rows(gcge_gpu_ctx *ctx, gcge_gpu_mat *A, const int *rowptr)
 {
-    long cnt = 0, nz = 0;
+    long cnt = 0;
     for (int r = 0; r < A->n; ++r)
         if (rowptr[r + 1] - rowptr[r] > GB_LONG_ROW) ++cnt;
     if (!cnt) return 0;
     int *h = (int *)malloc(sizeof(int) * cnt);
     if (!h) return 1;
-    cnt = 0;
-    for (int r = 0; r < A->n; ++r) {
-        const int len = rowptr[r + 1] - rowptr[r];
-        if (len > GB_LONG_ROW) {
-            h[cnt++] = r;
-            nz += len;
-        }
-    }
-    std::sort(h, h + cnt, [rowptr](int a, int b) {
-        const int la = rowptr[a + 1] - rowptr[a], lb = rowptr[b + 1] - rowptr[b];
-        return la != lb ? la > lb : a < b;
-    });
+    long nz = 0;
+    gb_long_rows_host(A->n, rowptr, GB_LONG_ROW, h, &nz);
     int rc = cudaMalloc(&A->lrows, sizeof(int) * cnt) != cudaSuccess ||
              cudaMemcpyAsync(A->lrows, h, sizeof(int) * cnt, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
              cudaStreamSynchronize(ctx->stream) != cudaSuccess;

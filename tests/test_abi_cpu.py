@@ -78,3 +78,27 @@ def test_python_structs_match_c_headers():
         a, b = map(int, subprocess.check_output([exe]).split())
     assert C.sizeof(G.Params) == a
     assert C.sizeof(G.Stats) == b
+
+
+def test_long_row_list_host_logic():
+    """The host pass that lists the rows the FP32 block-CG SpMM gives a block
+    each: rows longer than the threshold, longest first, ties by row index, and
+    their entry count (no GPU: a host function of the library)."""
+    import numpy as np
+    L = G.load()
+    L.gb_long_rows_host.restype = C.c_int
+    L.gb_long_rows_host.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_long)]
+    rng = np.random.default_rng(5)
+    for n, thresh in ((1, 0), (50, 64), (5000, 64), (5000, 5)):
+        lens = rng.integers(0, 200, n).astype(np.int32)
+        lens[rng.integers(0, n, max(1, n // 10))] = 130             # ties
+        rp = np.zeros(n + 1, dtype=np.int32)
+        rp[1:] = np.cumsum(lens)
+        out = np.full(n, -1, dtype=np.int32)
+        nz = C.c_long(-1)
+        cnt = L.gb_long_rows_host(n, rp.ctypes.data, thresh, out.ctypes.data, C.byref(nz))
+        want = [r for r in range(n) if lens[r] > thresh]
+        want.sort(key=lambda r: (-int(lens[r]), r))
+        assert cnt == len(want)
+        assert out[:cnt].tolist() == want
+        assert nz.value == int(sum(int(lens[r]) for r in want))
