@@ -232,11 +232,12 @@ extern "C" size_t gb_bcg_work_bytes(int n, int k, int precision)
 }
 
 // ---------------------------------------------------------------- FP32 rounds, fused
-// The FP32 (mixed-precision) rounds run on float4 kernels with a fixed grid of
-// VB_G blocks: block b always owns the same rows, so the per-block partial sums
-// and their fixed-order column sums are deterministic. A round is five launches:
-// p update, SpMM with the p.w partials in its epilogue, alpha, x/r update with
-// the r.r partials, beta and the active count.
+// The FP32 (mixed-precision) rounds (up to 256 columns) run on float4 kernels
+// with fixed grids: block b always owns the same rows, so the per-block partial
+// sums and their fixed-order column sums are deterministic. A round is five
+// launches -- p update, SpMM with the p.w partials in its epilogue, alpha, x/r
+// update with the r.r partials, beta and the active count -- plus a sixth for
+// matrices with rows longer than GB_LONG_ROW (their SpMM rows, a block each).
 #define VB_THREADS 256
 
 // Blocks of a grid-stride kernel of the fused rounds: the blocks that are resident
