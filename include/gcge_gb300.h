@@ -68,8 +68,11 @@ int  GCGE_GPU_Synchronize(gcge_gpu_ctx *ctx);
 
 /* Upload an n x n CSR matrix (RowPtr[n+1], KCol[nnz], Entries[nnz], as CSR_MAT,
  * app/csr/gcge_app_csr.h:27-40). keep_fp32 != 0 also keeps an FP32 copy of the
- * values for the mixed-precision inner solve. The structure is validated on the
- * host first (GCGE_GPU_ERR_CSR). */
+ * values for the mixed-precision inner solve, and lists the rows longer than 64
+ * entries (one host pass over rowptr) for the FP32 product, which gives each of
+ * them a block. The structure is checked on the device after the upload
+ * (GCGE_GPU_ERR_CSR: rowptr[0] != 0, a decreasing row pointer or a column index
+ * outside [0, n)). */
 int  GCGE_GPU_MatCreate(gcge_gpu_ctx *ctx, int n, const int *rowptr, const int *col,
                         const double *val, int keep_fp32, gcge_gpu_mat **A);
 /* Replace the values (same pattern); refreshes the FP32 copy if kept. */
