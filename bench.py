@@ -301,6 +301,7 @@ BIG_ESTIMATE_S = {0: {"c3": 500, "c5": 500}, 1: {"c3": 100, "c5": 180}}
 
 def run_gb300(args, dist):
     import gcge_gb300 as G
+    from gcge_gb300 import problems as P
     t_run = time.time()
     rank = dist.rank
     A, B, nev, block, exact, gen_s = make_problem(args.workload)
@@ -361,18 +362,31 @@ def run_gb300(args, dist):
         r2, _ = check_solution(A, B, ev2, X2, exact)
         p2 = {"s": sig(st2.solve_ms * 1e-3), "iters": st2.num_iter, "max_res": sig(r2, 3),
               "max_rel_ev_diff_vs_fp64": sig(float(np.max(np.abs(ev2 - ev64) / ev64)), 3)}
-    # ---- end to end through the host-buffer C ABI call (uploads + solve + download timed)
+    # ---- end to end through the host-buffer C ABI call (uploads + solve + download timed),
+    # from page-locked copies of the CSR arrays into a page-locked eigenvector buffer
+    # (made before the timed region; pageable arrays if pinning is not available)
     e2e = [float("nan")] if args.e2e_steps == 0 else []
     h2d = A.rowptr.nbytes + A.col.nbytes + A.val.nbytes + B.rowptr.nbytes + B.col.nbytes + B.val.nbytes
     d2h = A.n * nev * 8 + nev * 8
+    host_bufs = "pageable"
+    Ah, Bh, Xh_out, keep = A, B, None, []
+    if args.e2e_steps:
+        try:
+            Ah = P.CSR(*(pinned(a, keep) for a in (A.rowptr, A.col, A.val)))
+            Bh = P.CSR(*(pinned(a, keep) for a in (B.rowptr, B.col, B.val)))
+            Xh_out = pinned(np.zeros((nev, A.n)), keep)
+            host_bufs = "pinned"
+        except Exception:
+            Ah, Bh, Xh_out, keep = A, B, None, []
     for i in range((1 + args.e2e_steps) if args.e2e_steps else 0):
         p = params(args.precision)
         ctx.sync()
         t = time.time()
-        ctx.solve_host(A, B, p)
+        ctx.solve_host(Ah, Bh, p, out=Xh_out)
         if i >= 1:
             e2e.append(time.time() - t)
     e2e_s = dist.max(sum(e2e) / len(e2e))
+    del Ah, Bh, Xh_out, keep
     # ---- supplementary: the same mixed solve with the Jacobi-preconditioned inner block CG
     # (the role of a solver installed in ops->LinearSolver); not the headline, which keeps
     # the reference's plain block CG
@@ -449,7 +463,8 @@ def run_gb300(args, dist):
                        "l2": "inputs larger than L2 (A+B %.0f MB > 129 MB)" % (h2d / 1e6),
                        "why_not_c3": "the 160^3 mixed config takes ~2 min per solve; it is solved once per run "
                                      "(key c3), not K times"},
-            "e2e": {"value": sig(e2e_s), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "e2e": {"value": sig(e2e_s), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "host_buffers": host_bufs},
             "gpu_launches": int(launches),
             "roofline": {"kernel": dom, "bound": "hbm" if d["bound"] != "tensor" else "tensor",
                          "achieved": sig(d["achieved_gbs"]) if d["bound"] != "tensor" else sig(
@@ -508,6 +523,19 @@ def run_reference(args, dist):
                              "sample": "%d complete solves of the oracle port on the 2-D Laplacian 100x100 "
                                        "(n=10000, nev=10, BR<=1e-8, %d iterations)" % (d["solves"], d["iters"])},
             "e2e": {"value": None, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def pinned(arr, keep):
+    """A copy of arr in page-locked host memory (torch's pinned allocator); the
+    owning tensor is appended to keep, which must outlive the copy's use. Raises
+    where no CUDA device is present."""
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
+    keep.append(t)
+    out = t.numpy()
+    if not np.array_equal(out.ravel()[:64], np.ascontiguousarray(arr).ravel()[:64]):
+        raise RuntimeError("pinned copy differs")
+    return out
 
 
 def run_kernel(args):

@@ -258,11 +258,18 @@ class Context:
         out = X.download(0, nev)
         return ev, out, st
 
-    def solve_host(self, A, B, params, init=None):
-        """Host-buffer entry (uploads, solves, downloads). A, B: problems.CSR."""
+    def solve_host(self, A, B, params, init=None, out=None):
+        """Host-buffer entry (uploads, solves, downloads). A, B: problems.CSR.
+        out: optional C-contiguous float64 (nev, n) host array (page-locked, say)
+        that receives the eigenvectors, one per row."""
         nev = params.nev
         ev = np.zeros(nev)
-        X = np.zeros((nev, A.n))
+        if out is not None:
+            if out.dtype != np.float64 or out.shape != (nev, A.n) or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError("out must be a C-contiguous float64 array of shape (nev, n)")
+            X = out
+        else:
+            X = np.zeros((nev, A.n))
         if init is not None:
             X[:] = np.asarray(init, dtype=np.float64).T
             params.given_init_evec = 1
