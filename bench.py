@@ -372,9 +372,9 @@ def run_gb300(args, dist):
     Ah, Bh, Xh_out, keep = A, B, None, []
     if args.e2e_steps:
         try:
-            Ah = P.CSR(*(pinned(a, keep) for a in (A.rowptr, A.col, A.val)))
-            Bh = P.CSR(*(pinned(a, keep) for a in (B.rowptr, B.col, B.val)))
-            Xh_out = pinned(np.zeros((nev, A.n)), keep)
+            Ah = P.CSR(*(pinned(a, keep, dist.local) for a in (A.rowptr, A.col, A.val)))
+            Bh = P.CSR(*(pinned(a, keep, dist.local) for a in (B.rowptr, B.col, B.val)))
+            Xh_out = pinned(np.zeros((nev, A.n)), keep, dist.local)
             host_bufs = "pinned"
         except Exception:
             Ah, Bh, Xh_out, keep = A, B, None, []
@@ -525,11 +525,13 @@ def run_reference(args, dist):
             "e2e": {"value": None, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def pinned(arr, keep):
-    """A copy of arr in page-locked host memory (torch's pinned allocator); the
-    owning tensor is appended to keep, which must outlive the copy's use. Raises
-    where no CUDA device is present."""
+def pinned(arr, keep, device=0):
+    """A copy of arr in page-locked host memory (torch's pinned allocator, with
+    torch bound to this rank's GPU so that no rank opens a context on another);
+    the owning tensor is appended to keep, which must outlive the copy's use.
+    Raises where no CUDA device is present."""
     import torch
+    torch.cuda.set_device(device)
     t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
     keep.append(t)
     out = t.numpy()
